@@ -1,0 +1,610 @@
+// C ABI of libgls: context, netlist upload, stimulus windows, level loop.
+//
+// The run of one window replaces the per-level host loop of the reference
+// GPU tool (src/simulate.cu:2027-3254).  Nothing goes back to the host
+// between levels: every net's change list stays in the device event pool,
+// and a level's fan-in is read in place by the next level's kernels.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+#include "gls.h"
+#include "gls_internal.h"
+
+using namespace gls;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, n ? n : 16);
+        if (e == cudaSuccess) bytes = n ? n : 16;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Window {
+    std::vector<uint32_t> stim_nets;
+    std::vector<uint64_t> stim_off;     // aligned pool offset per stimulus net
+    std::vector<uint32_t> stim_len;
+    uint64_t stim_events = 0;           // aligned extent of the stimulus in the pool
+    std::vector<uint32_t> h_time;       // packed stimulus (kept to re-upload on pool growth)
+    std::vector<uint8_t> h_value;
+    uint64_t t_begin = 0, t_end = 0;
+    uint64_t cap = 0;
+    DevBuf pool_t, pool_v, net_off, net_len, init_off, init_len, saif, small, stim_dev;
+    bool done = false;
+};
+
+}  // namespace
+
+struct gls_ctx {
+    gls_opts opts{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int sm_count = 0;
+    std::string err;
+    bool loaded = false;
+    uint32_t n_nets = 0;
+    uint32_t n_drv = 0;
+    std::vector<uint32_t> drv_level_start;   // per level, into drivers
+    uint32_t max_width = 0;
+    uint64_t pins_total = 0;
+    std::vector<uint8_t> driven;             // net driven by a gate output
+    std::vector<uint32_t> ext_inputs;        // nets read by gates and driven by no gate
+    DevBuf meta, arcs, lut;
+    DevBuf seg_base, slot, segs;
+    uint32_t seg_cap = 0;
+    uint32_t def_delay = 1;
+    std::vector<Window *> windows;
+    gls_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int fail(gls_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+int cuda_fail(gls_ctx *c, cudaError_t e, const char *what)
+{
+    return fail(c, e == cudaErrorMemoryAllocation ? GLS_ENOMEM : GLS_ECUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                        \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+uint64_t round4(uint64_t x) { return (x + 3) & ~3ull; }
+
+}  // namespace
+
+extern "C" int gls_abi_version(void) { return GLS_ABI_VERSION; }
+
+extern "C" const char *gls_last_error(const gls_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
+{
+    if (!out) return GLS_EINVAL;
+    *out = nullptr;
+    gls_ctx *ctx = new gls_ctx();
+    if (opts) ctx->opts = *opts;
+    else {
+        ctx->opts.delay_factor = 1.0;
+    }
+    if (ctx->opts.delay_factor <= 0.0) ctx->opts.delay_factor = 1.0;
+    if (ctx->opts.calc_mode != GLS_CALC_FIXED && ctx->opts.calc_mode != GLS_CALC_LITERAL) {
+        delete ctx;
+        return GLS_EINVAL;
+    }
+    if (!ctx->opts.seg_events) ctx->opts.seg_events = 256;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0 || ctx->opts.device < 0 || ctx->opts.device >= ndev) {
+        delete ctx;
+        return GLS_ECUDA;
+    }
+    e = cudaSetDevice(ctx->opts.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->opts.device);
+    if (e == cudaSuccess) {
+        if (ctx->opts.stream) ctx->stream = (cudaStream_t)ctx->opts.stream;
+        else {
+            e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+            ctx->own_stream = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return GLS_ECUDA;
+    }
+    ctx->def_delay = (uint32_t)(uint64_t)(1.0 * ctx->opts.delay_factor);
+    *out = ctx;
+    return GLS_OK;
+}
+
+static void free_window(Window *w)
+{
+    w->pool_t.release(); w->pool_v.release(); w->net_off.release(); w->net_len.release();
+    w->init_off.release(); w->init_len.release(); w->saif.release(); w->small.release();
+    w->stim_dev.release();
+    delete w;
+}
+
+extern "C" int gls_clear_windows(gls_ctx *ctx)
+{
+    if (!ctx) return GLS_EINVAL;
+    cudaSetDevice(ctx->opts.device);
+    cudaStreamSynchronize(ctx->stream);
+    for (Window *w : ctx->windows) free_window(w);
+    ctx->windows.clear();
+    return GLS_OK;
+}
+
+extern "C" int gls_destroy(gls_ctx *ctx)
+{
+    if (!ctx) return GLS_EINVAL;
+    gls_clear_windows(ctx);
+    ctx->meta.release(); ctx->arcs.release(); ctx->lut.release();
+    ctx->seg_base.release(); ctx->slot.release(); ctx->segs.release();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GLS_OK;
+}
+
+extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
+{
+    if (!ctx || !nl) return GLS_EINVAL;
+    if (!nl->cells || !nl->prims || !nl->level_start || !nl->inst_cell || !nl->inst_pin_start ||
+        !nl->inst_pin_net || !nl->inst_arc_start || (!nl->arcs && nl->inst_arc_start[nl->n_inst]))
+        return fail(ctx, GLS_EINVAL, "netlist: null array");
+    cudaSetDevice(ctx->opts.device);
+    if (nl->level_start[0] != 0 || nl->level_start[nl->n_levels] != nl->n_inst)
+        return fail(ctx, GLS_EINVAL, "netlist: level_start must span all instances");
+    for (uint32_t c = 0; c < nl->n_cells; ++c) {
+        const gls_cell &cl = nl->cells[c];
+        if (cl.n_in > kMaxPins) return fail(ctx, GLS_EINVAL, "cell %u: %u inputs (max %d)", c, cl.n_in, kMaxPins);
+        if ((uint64_t)cl.prim_start + cl.n_prim > nl->n_prims) return fail(ctx, GLS_EINVAL, "cell %u: primitive range", c);
+    }
+    // truth tables, one per (cell, output), built on first use
+    std::map<std::pair<uint32_t, int>, uint32_t> lut_of;
+    std::vector<uint8_t> h_lut;
+    std::vector<DrvMeta> h_meta;
+    std::vector<ArcDev> h_arcs;
+    std::vector<int32_t> drv_level_of_net(nl->n_nets, -1);
+    ctx->drv_level_start.assign(1, 0);
+    ctx->pins_total = 0;
+    std::vector<uint8_t> consumed(nl->n_nets, 0);
+    for (uint32_t L = 0; L < nl->n_levels; ++L) {
+        for (uint32_t i = nl->level_start[L]; i < nl->level_start[L + 1]; ++i) {
+            const uint32_t cid = nl->inst_cell[i];
+            if (cid >= nl->n_cells) return fail(ctx, GLS_EINVAL, "instance %u: bad cell", i);
+            const gls_cell &cl = nl->cells[cid];
+            const uint32_t p0 = nl->inst_pin_start[i];
+            if (nl->inst_pin_start[i + 1] - p0 != (uint32_t)cl.n_in + cl.n_out)
+                return fail(ctx, GLS_EINVAL, "instance %u: pin count", i);
+            const uint32_t *pins = nl->inst_pin_net + p0;
+            DrvMeta md;
+            std::memset(&md, 0, sizeof md);
+            int m = 0;
+            bool ident = true;
+            for (int p = 0; p < cl.n_in; ++p) {
+                const uint32_t net = pins[p];
+                if (net >= nl->n_nets) return fail(ctx, GLS_EINVAL, "instance %u: bad net", i);
+                consumed[net] = 1;
+                int slotp = -1;
+                for (int j = 0; j < m; ++j) if (md.net[j] == net) slotp = j;
+                if (slotp < 0) {
+                    if (m == kMaxSlots) return fail(ctx, GLS_EINVAL, "instance %u: too many fan-in nets", i);
+                    md.net[m] = net;
+                    slotp = m++;
+                }
+                if (slotp != p) ident = false;
+                md.pin_slot |= (uint32_t)slotp << (3 * p);
+                if (drv_level_of_net[net] >= (int32_t)L)
+                    return fail(ctx, GLS_EINVAL, "instance %u (level %u) reads net %u produced at level %d", i, L, net,
+                                drv_level_of_net[net]);
+            }
+            md.m = (uint8_t)m;
+            md.n_pins = cl.n_in;
+            md.ident = ident ? 1 : 0;
+            ctx->pins_total += cl.n_in;
+            for (int o = 0; o < cl.n_out; ++o) {
+                DrvMeta d = md;
+                const uint32_t onet = pins[cl.n_in + o];
+                if (onet >= nl->n_nets) return fail(ctx, GLS_EINVAL, "instance %u: bad output net", i);
+                if (drv_level_of_net[onet] >= 0) return fail(ctx, GLS_EINVAL, "net %u has two drivers", onet);
+                drv_level_of_net[onet] = (int32_t)L;
+                d.out_net = onet;
+                d.reserved = o == 0 ? 1u : 0u;
+                auto key = std::make_pair(cid, o);
+                auto it = lut_of.find(key);
+                if (it == lut_of.end()) {
+                    const uint32_t off = (uint32_t)h_lut.size();
+                    h_lut.resize(off + (1u << (2 * cl.n_in)));
+                    int rc = gls_cell_lut(&cl, nl->prims, o, ctx->opts.calc_mode, h_lut.data() + off,
+                                          1u << (2 * cl.n_in));
+                    if (rc) return fail(ctx, rc, "cell %u: bad primitive program", cid);
+                    it = lut_of.emplace(key, off).first;
+                }
+                d.lut_off = it->second;
+                d.arc_off = (uint32_t)h_arcs.size();
+                uint32_t na = 0;
+                for (uint32_t a = nl->inst_arc_start[i]; a < nl->inst_arc_start[i + 1]; ++a) {
+                    const gls_arc &A = nl->arcs[a];
+                    if (A.out_pin != o) continue;
+                    if (A.edge > 2) return fail(ctx, GLS_EINVAL, "instance %u: arc edge %u", i, A.edge);
+                    if (A.in_pin >= cl.n_in) continue;   // never related: its net is not an input
+                    const uint32_t slotp = (md.pin_slot >> (3 * A.in_pin)) & 7u;
+                    const double r = A.rise * ctx->opts.delay_factor, f = A.fall * ctx->opts.delay_factor;
+                    if (!(r >= 0.0) || !(f >= 0.0) || r >= 4294967295.0 || f >= 4294967295.0)
+                        return fail(ctx, GLS_ERANGE, "instance %u: delay out of range", i);
+                    ArcDev ad;
+                    ad.info = (uint32_t)A.edge | (slotp << 2);
+                    ad.rise = (uint32_t)(uint64_t)r;
+                    ad.fall = (uint32_t)(uint64_t)f;
+                    ad.pad = 0;
+                    h_arcs.push_back(ad);
+                    ++na;
+                }
+                if (na > 255) return fail(ctx, GLS_EINVAL, "instance %u: too many arcs", i);
+                d.n_arcs = (uint8_t)na;
+                h_meta.push_back(d);
+            }
+        }
+        ctx->drv_level_start.push_back((uint32_t)h_meta.size());
+    }
+    ctx->n_nets = nl->n_nets;
+    ctx->n_drv = (uint32_t)h_meta.size();
+    ctx->max_width = 0;
+    for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L)
+        ctx->max_width = std::max(ctx->max_width, ctx->drv_level_start[L + 1] - ctx->drv_level_start[L]);
+    ctx->driven.assign(nl->n_nets, 0);
+    ctx->ext_inputs.clear();
+    for (uint32_t n = 0; n < nl->n_nets; ++n) {
+        ctx->driven[n] = drv_level_of_net[n] >= 0;
+        if (consumed[n] && !ctx->driven[n]) ctx->ext_inputs.push_back(n);
+    }
+    if (h_arcs.empty()) h_arcs.push_back(ArcDev{0, 0, 0, 0});
+    if (h_lut.empty()) h_lut.push_back(kVX);
+    if (h_meta.empty()) h_meta.push_back(DrvMeta{});
+    CK(ctx->meta.ensure(h_meta.size() * sizeof(DrvMeta)), "alloc meta");
+    CK(ctx->arcs.ensure(h_arcs.size() * sizeof(ArcDev)), "alloc arcs");
+    CK(ctx->lut.ensure(h_lut.size()), "alloc lut");
+    CK(cudaMemcpy(ctx->meta.p, h_meta.data(), h_meta.size() * sizeof(DrvMeta), cudaMemcpyHostToDevice), "upload meta");
+    CK(cudaMemcpy(ctx->arcs.p, h_arcs.data(), h_arcs.size() * sizeof(ArcDev), cudaMemcpyHostToDevice), "upload arcs");
+    CK(cudaMemcpy(ctx->lut.p, h_lut.data(), h_lut.size(), cudaMemcpyHostToDevice), "upload lut");
+    CK(ctx->seg_base.ensure((size_t)(ctx->max_width + 1) * 4), "alloc seg_base");
+    CK(ctx->slot.ensure((size_t)(ctx->max_width + 1) * 8), "alloc slot");
+    ctx->seg_cap = std::max<uint32_t>(1u << 20, 8 * ctx->max_width + 64);
+    CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "alloc segs");
+    ctx->loaded = true;
+    return GLS_OK;
+}
+
+static int upload_window(gls_ctx *ctx, Window *w)
+{
+    const uint64_t n = ctx->n_nets;
+    CK(w->pool_t.ensure(w->cap * 4), "alloc pool times");
+    CK(w->pool_v.ensure(w->cap), "alloc pool values");
+    CK(w->net_off.ensure(n * 8), "alloc net_off");
+    CK(w->net_len.ensure(n * 4), "alloc net_len");
+    CK(w->init_off.ensure(n * 8), "alloc init_off");
+    CK(w->init_len.ensure(n * 4), "alloc init_len");
+    CK(w->saif.ensure(n * 24), "alloc saif");
+    CK(w->small.ensure(256), "alloc counters");
+    CK(w->stim_dev.ensure(w->stim_nets.size() * 4), "alloc stim nets");
+    if (w->stim_events) {
+        CK(cudaMemcpyAsync(w->pool_t.p, w->h_time.data(), w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
+           "upload stimulus times");
+        CK(cudaMemcpyAsync(w->pool_v.p, w->h_value.data(), w->stim_events, cudaMemcpyHostToDevice, ctx->stream),
+           "upload stimulus values");
+    }
+    std::vector<uint64_t> off(n, 0);
+    std::vector<uint32_t> len(n, 0xFFFFFFFFu);
+    for (size_t k = 0; k < w->stim_nets.size(); ++k) {
+        off[w->stim_nets[k]] = w->stim_off[k];
+        len[w->stim_nets[k]] = w->stim_len[k];
+    }
+    CK(cudaMemcpyAsync(w->init_off.p, off.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream), "upload offsets");
+    CK(cudaMemcpyAsync(w->init_len.p, len.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "upload lengths");
+    if (!w->stim_nets.empty())
+        CK(cudaMemcpyAsync(w->stim_dev.p, w->stim_nets.data(), w->stim_nets.size() * 4, cudaMemcpyHostToDevice,
+                           ctx->stream),
+           "upload stim nets");
+    CK(cudaStreamSynchronize(ctx->stream), "upload sync");
+    return GLS_OK;
+}
+
+extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_begin, uint64_t t_end,
+                              uint32_t *window_id)
+{
+    if (!ctx || !st) return GLS_EINVAL;
+    if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "add_window before load_netlist");
+    if (t_end <= t_begin) return fail(ctx, GLS_EINVAL, "window end %llu must exceed begin %llu",
+                                      (unsigned long long)t_end, (unsigned long long)t_begin);
+    if (st->n_nets && (!st->net || !st->ev_start || !st->time || !st->value))
+        return fail(ctx, GLS_EINVAL, "stimulus: null array");
+    cudaSetDevice(ctx->opts.device);
+    Window *w = new Window();
+    w->t_begin = t_begin;
+    w->t_end = t_end;
+    std::vector<uint8_t> seen(ctx->n_nets, 0);
+    uint64_t total = 0, maxlen = 0;
+    for (uint32_t k = 0; k < st->n_nets; ++k) {
+        const uint32_t net = st->net[k];
+        if (net >= ctx->n_nets) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u out of range", net); }
+        if (seen[net]) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u given twice", net); }
+        if (ctx->driven[net]) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u is driven by a gate", net); }
+        seen[net] = 1;
+        const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
+        if (b < a) { delete w; return fail(ctx, GLS_EINVAL, "stimulus ev_start not monotone"); }
+        for (uint64_t e = a; e < b; ++e) {
+            if (st->value[e] > 3) { delete w; return fail(ctx, GLS_EINVAL, "stimulus value %u", st->value[e]); }
+            if (st->time[e] == 0xFFFFFFFFu) { delete w; return fail(ctx, GLS_ERANGE, "stimulus time 2^32-1"); }
+            if (e > a && st->time[e] <= st->time[e - 1]) {
+                delete w;
+                return fail(ctx, GLS_EINVAL, "stimulus net %u: times not strictly increasing", net);
+            }
+        }
+        total += round4(b - a);
+        maxlen = std::max<uint64_t>(maxlen, b - a);
+    }
+    for (uint32_t net : ctx->ext_inputs)
+        if (!seen[net]) { delete w; return fail(ctx, GLS_EINVAL, "net %u is read by a gate but has no stimulus", net); }
+    // pack the stimulus into the pool layout (each net on a 4-event boundary)
+    w->stim_nets.assign(st->net, st->net + st->n_nets);
+    w->stim_off.resize(st->n_nets);
+    w->stim_len.resize(st->n_nets);
+    w->h_time.assign(total, 0);
+    w->h_value.assign(total, kVX);
+    uint64_t at = 0;
+    for (uint32_t k = 0; k < st->n_nets; ++k) {
+        const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
+        w->stim_off[k] = at;
+        w->stim_len[k] = (uint32_t)(b - a);
+        if (b > a) {
+            std::memcpy(w->h_time.data() + at, st->time + a, (b - a) * 4);
+            std::memcpy(w->h_value.data() + at, st->value + a, b - a);
+        }
+        at += round4(b - a);
+    }
+    w->stim_events = total;
+    // initial pool capacity: stimulus plus an estimate of every gate's slot
+    uint64_t cap = ctx->opts.pool_events;
+    if (!cap) {
+        const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
+        cap = total + (uint64_t)(1.5 * avg * (double)ctx->pins_total) + 8ull * ctx->n_drv + 1024;
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+            const uint64_t limit = (uint64_t)(fr * 0.6) / 5;
+            if (cap > limit) cap = std::max<uint64_t>(limit, total + 1024);
+        }
+    }
+    w->cap = std::max<uint64_t>(cap, total + 1024);
+    int rc = upload_window(ctx, w);
+    if (rc) { free_window(w); return rc; }
+    ctx->windows.push_back(w);
+    if (window_id) *window_id = (uint32_t)(ctx->windows.size() - 1);
+    return GLS_OK;
+}
+
+static WinDev make_windev(gls_ctx *ctx, Window *w)
+{
+    WinDev d;
+    d.net_off = w->net_off.as<uint64_t>();
+    d.net_len = w->net_len.as<uint32_t>();
+    d.pool_t = w->pool_t.as<uint32_t>();
+    d.pool_v = w->pool_v.as<uint8_t>();
+    d.saif = w->saif.as<unsigned long long>();
+    unsigned long long *sm = w->small.as<unsigned long long>();
+    d.top = sm;
+    d.counters = sm + 1;     // 3 counters
+    d.err = reinterpret_cast<uint32_t *>(sm + 4);
+    d.n_segs = reinterpret_cast<uint32_t *>(sm + 5);
+    d.seg_base = ctx->seg_base.as<uint32_t>();
+    d.slot = ctx->slot.as<uint64_t>();
+    d.segs = ctx->segs.as<SegRec>();
+    d.cap = w->cap;
+    d.seg_cap = ctx->seg_cap;
+    d.t_begin = w->t_begin;
+    d.t_end = w->t_end;
+    return d;
+}
+
+static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
+{
+    const uint64_t n = ctx->n_nets;
+    CK(cudaMemcpyAsync(w->net_off.p, w->init_off.p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "reset offsets");
+    CK(cudaMemcpyAsync(w->net_len.p, w->init_len.p, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "reset lengths");
+    CK(cudaMemsetAsync(w->saif.p, 0xFF, n * 24, ctx->stream), "reset saif");
+    unsigned long long small[8] = {w->stim_events, 0, 0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(w->small.p, small, sizeof small, cudaMemcpyHostToDevice, ctx->stream), "reset counters");
+    WinDev d = make_windev(ctx, w);
+    launch_stim_saif(d, w->stim_dev.as<uint32_t>(), (uint32_t)w->stim_nets.size(), ctx->stream);
+    ++*launches;
+    LevelArgs a;
+    a.meta = ctx->meta.as<DrvMeta>();
+    a.arcs = ctx->arcs.as<ArcDev>();
+    a.lut = ctx->lut.as<uint8_t>();
+    a.seg_events = ctx->opts.seg_events;
+    a.def_delay = ctx->def_delay;
+    for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
+        a.lo = ctx->drv_level_start[L];
+        a.hi = ctx->drv_level_start[L + 1];
+        launch_level(d, a, ctx->sm_count, ctx->stream, launches);
+    }
+    CK(cudaGetLastError(), "kernel launch");
+    return GLS_OK;
+}
+
+extern "C" int gls_run(gls_ctx *ctx)
+{
+    if (!ctx) return GLS_EINVAL;
+    if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "run before load_netlist");
+    cudaSetDevice(ctx->opts.device);
+    uint32_t launches = 0;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+    for (Window *w : ctx->windows) {
+        int rc = enqueue_window(ctx, w, &launches);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "run");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    double total_ms = ms;
+    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0;
+    // check every window; regrow the pool or the segment table and rerun
+    for (Window *w : ctx->windows) {
+        for (int attempt = 0;; ++attempt) {
+            unsigned long long small[8];
+            CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
+            const uint32_t err = (uint32_t)small[4];
+            if (!err) {
+                gate_ev += small[1];
+                out_ev += small[2];
+                segs += small[3];
+                pool_ev += small[0];
+                pool_bytes += w->cap * 5;
+                break;
+            }
+            if (err & (kErrRegion | kErrEmptied | kErrTime)) {
+                return fail(ctx, err & kErrTime ? GLS_ERANGE : GLS_EINVAL,
+                            "simulation error flags 0x%x (%s)", err,
+                            err & kErrTime ? "output time reached 2^32-1"
+                                           : err & kErrEmptied ? "output list emptied by a zero delay at time 0"
+                                                               : "segment region overflow");
+            }
+            if (attempt > 12) return fail(ctx, GLS_EOVERFLOW, "event pool could not grow enough");
+            if (err & kErrSegCap) {
+                ctx->seg_cap *= 2;
+                CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "grow segs");
+            }
+            if (err & kErrPool) {
+                w->cap *= 2;
+                w->pool_t.release();
+                w->pool_v.release();
+                int rc = upload_window(ctx, w);
+                if (rc) return fail(ctx, GLS_EOVERFLOW, "event pool growth to %llu events failed: %s",
+                                    (unsigned long long)w->cap, ctx->err.c_str());
+                ctx->stats.overflow_retries++;
+            }
+            uint32_t l2 = 0;
+            CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+            int rc = enqueue_window(ctx, w, &l2);
+            if (rc) return rc;
+            CK(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+            CK(cudaStreamSynchronize(ctx->stream), "rerun");
+            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+            total_ms += ms;
+            launches += l2;
+        }
+        w->done = true;
+    }
+    ctx->stats.gate_events = gate_ev;
+    ctx->stats.output_events = out_ev;
+    ctx->stats.segments = segs;
+    ctx->stats.pool_events = pool_ev;
+    ctx->stats.pool_bytes = pool_bytes;
+    ctx->stats.kernel_ms = total_ms;
+    ctx->stats.launches = launches;
+    ctx->stats.n_windows = (uint32_t)ctx->windows.size();
+    return GLS_OK;
+}
+
+static Window *get_done(gls_ctx *ctx, uint32_t window)
+{
+    if (window >= ctx->windows.size()) return nullptr;
+    Window *w = ctx->windows[window];
+    return w->done ? w : nullptr;
+}
+
+extern "C" int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint64_t *t1, uint64_t *tx)
+{
+    if (!ctx || !t0 || !t1 || !tx) return GLS_EINVAL;
+    Window *w = get_done(ctx, window);
+    if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
+    cudaSetDevice(ctx->opts.device);
+    std::vector<uint64_t> buf((size_t)ctx->n_nets * 3);
+    CK(cudaMemcpy(buf.data(), w->saif.p, buf.size() * 8, cudaMemcpyDeviceToHost), "read saif");
+    for (uint32_t n = 0; n < ctx->n_nets; ++n) {
+        t0[n] = buf[3ull * n];
+        t1[n] = buf[3ull * n + 1];
+        tx[n] = buf[3ull * n + 2];
+    }
+    return GLS_OK;
+}
+
+extern "C" int gls_waveform_lengths(gls_ctx *ctx, uint32_t window, uint32_t *len)
+{
+    if (!ctx || !len) return GLS_EINVAL;
+    Window *w = get_done(ctx, window);
+    if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
+    cudaSetDevice(ctx->opts.device);
+    CK(cudaMemcpy(len, w->net_len.p, (size_t)ctx->n_nets * 4, cudaMemcpyDeviceToHost), "read lengths");
+    return GLS_OK;
+}
+
+extern "C" int gls_waveform(gls_ctx *ctx, uint32_t window, uint32_t net, uint32_t *time, uint8_t *value,
+                            uint64_t cap, uint64_t *n)
+{
+    if (!ctx || !n) return GLS_EINVAL;
+    Window *w = get_done(ctx, window);
+    if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
+    if (net >= ctx->n_nets) return fail(ctx, GLS_EINVAL, "net %u out of range", net);
+    cudaSetDevice(ctx->opts.device);
+    uint64_t off = 0;
+    uint32_t len = 0;
+    CK(cudaMemcpy(&off, w->net_off.as<uint64_t>() + net, 8, cudaMemcpyDeviceToHost), "read offset");
+    CK(cudaMemcpy(&len, w->net_len.as<uint32_t>() + net, 4, cudaMemcpyDeviceToHost), "read length");
+    if (len == 0xFFFFFFFFu) {
+        *n = UINT64_MAX;
+        return GLS_OK;
+    }
+    *n = len;
+    const uint64_t k = std::min<uint64_t>(cap, len);
+    if (k && time) CK(cudaMemcpy(time, w->pool_t.as<uint32_t>() + off, k * 4, cudaMemcpyDeviceToHost), "read times");
+    if (k && value) CK(cudaMemcpy(value, w->pool_v.as<uint8_t>() + off, k, cudaMemcpyDeviceToHost), "read values");
+    return GLS_OK;
+}
+
+extern "C" int gls_stats_get(gls_ctx *ctx, gls_stats *st)
+{
+    if (!ctx || !st) return GLS_EINVAL;
+    *st = ctx->stats;
+    return GLS_OK;
+}

@@ -1,0 +1,210 @@
+"""ctypes binding of the C ABI declared in include/gls.h.
+
+This is the reference-facing boundary: `Simulator` mirrors the reference's
+simulate stage (load the levelized netlist, take a stimulus window, run the
+levels, read SAIF counts and waveforms).  There is no CPU fallback: if
+libgls.so is missing or no CUDA device is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .netlist import Netlist, Stimulus
+
+LIB_PATH = Path(__file__).resolve().parent.parent / "lib" / "libgls.so"
+
+GLS_OK, GLS_EINVAL, GLS_ECUDA, GLS_ENOMEM, GLS_ESTATE, GLS_ERANGE, GLS_EOVERFLOW = range(7)
+CALC_FIXED, CALC_LITERAL = 0, 1
+ALLOC_BOUND, ALLOC_EXACT = 0, 1
+
+# every symbol include/gls.h declares
+EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "gls_add_window",
+            "gls_clear_windows", "gls_run", "gls_saif_counts", "gls_waveform_lengths", "gls_waveform",
+            "gls_stats_get", "gls_cell_lut", "gls_abi_version"]
+
+
+class GlsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gls error {code}: {msg}")
+        self.code = code
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int), ("calc_mode", C.c_int), ("alloc_mode", C.c_int),
+                ("delay_factor", C.c_double), ("seg_events", C.c_uint32), ("pool_events", C.c_uint64),
+                ("stream", C.c_void_p)]
+
+
+class NetlistC(C.Structure):
+    _fields_ = [("n_nets", C.c_uint32), ("n_cells", C.c_uint32), ("cells", C.c_void_p),
+                ("n_prims", C.c_uint32), ("prims", C.c_void_p), ("n_inst", C.c_uint32),
+                ("n_levels", C.c_uint32), ("level_start", C.c_void_p), ("inst_cell", C.c_void_p),
+                ("inst_pin_start", C.c_void_p), ("inst_pin_net", C.c_void_p),
+                ("inst_arc_start", C.c_void_p), ("arcs", C.c_void_p)]
+
+
+class StimulusC(C.Structure):
+    _fields_ = [("n_nets", C.c_uint32), ("net", C.c_void_p), ("ev_start", C.c_void_p),
+                ("time", C.c_void_p), ("value", C.c_void_p)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("gate_events", C.c_uint64), ("output_events", C.c_uint64), ("segments", C.c_uint64),
+                ("pool_events", C.c_uint64), ("pool_bytes", C.c_uint64), ("overflow_retries", C.c_uint64),
+                ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("n_windows", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: Path | None = None) -> C.CDLL:
+    """Load libgls.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: run __graft_entry__.build() (libgls is required, no fallback)")
+    lib = C.CDLL(str(p))
+    lib.gls_last_error.restype = C.c_char_p
+    lib.gls_last_error.argtypes = [C.c_void_p]
+    lib.gls_create.argtypes = [C.POINTER(Opts), C.POINTER(C.c_void_p)]
+    lib.gls_destroy.argtypes = [C.c_void_p]
+    lib.gls_load_netlist.argtypes = [C.c_void_p, C.POINTER(NetlistC)]
+    lib.gls_add_window.argtypes = [C.c_void_p, C.POINTER(StimulusC), C.c_uint64, C.c_uint64,
+                                   C.POINTER(C.c_uint32)]
+    lib.gls_clear_windows.argtypes = [C.c_void_p]
+    lib.gls_run.argtypes = [C.c_void_p]
+    lib.gls_saif_counts.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gls_waveform_lengths.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+    lib.gls_waveform.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
+                                 C.POINTER(C.c_uint64)]
+    lib.gls_stats_get.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    lib.gls_cell_lut.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint32]
+    lib.gls_abi_version.restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def cell_lut(cell_rec: np.ndarray, prims: np.ndarray, out: int, calc_mode: int) -> np.ndarray:
+    """Truth table of one cell output (host helper, no GPU needed)."""
+    lib = load_library()
+    rec = np.ascontiguousarray(cell_rec.copy())
+    rec["prim_start"] = 0
+    n = 1 << (2 * int(rec["n_in"]))
+    lut = np.zeros(n, np.uint8)
+    rc = lib.gls_cell_lut(_ptr(rec), _ptr(np.ascontiguousarray(prims)), out, calc_mode, _ptr(lut), n)
+    if rc:
+        raise GlsError(rc, "gls_cell_lut")
+    return lut
+
+
+class Simulator:
+    """One libgls context on one GPU: the simulate stage behind a C ABI."""
+
+    def __init__(self, device: int = 0, calc_mode: int = CALC_FIXED, seg_events: int = 0,
+                 pool_events: int = 0, delay_factor: float = 1.0, stream: int | None = None,
+                 alloc_mode: int = ALLOC_BOUND):
+        self.lib = load_library()
+        o = Opts(device, calc_mode, alloc_mode, delay_factor, seg_events, pool_events, stream or None)
+        h = C.c_void_p()
+        rc = self.lib.gls_create(C.byref(o), C.byref(h))
+        if rc:
+            raise GlsError(rc, "gls_create failed (no CUDA device?)")
+        self.h = h
+        self.n_nets = 0
+        self._keep = []
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise GlsError(rc, f"{what}: {self.lib.gls_last_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            self.lib.gls_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def load(self, nl: Netlist):
+        cells, prims = nl.cell_arrays()
+        arrs = dict(
+            cells=np.ascontiguousarray(cells), prims=np.ascontiguousarray(prims),
+            level_start=np.ascontiguousarray(nl.level_start, np.uint32),
+            inst_cell=np.ascontiguousarray(nl.inst_cell, np.uint32),
+            pin_start=np.ascontiguousarray(nl.pin_start, np.uint32),
+            pin_net=np.ascontiguousarray(nl.pin_net, np.uint32),
+            arc_start=np.ascontiguousarray(nl.arc_start, np.uint32),
+            arcs=np.ascontiguousarray(nl.arcs) if len(nl.arcs) else np.zeros(1, nl.arcs.dtype),
+        )
+        c = NetlistC(nl.n_nets, len(cells), _ptr(arrs["cells"]), len(prims), _ptr(arrs["prims"]), nl.n_inst,
+                     nl.n_levels, _ptr(arrs["level_start"]), _ptr(arrs["inst_cell"]), _ptr(arrs["pin_start"]),
+                     _ptr(arrs["pin_net"]), _ptr(arrs["arc_start"]), _ptr(arrs["arcs"]))
+        self._check(self.lib.gls_load_netlist(self.h, C.byref(c)), "load_netlist")
+        self.n_nets = nl.n_nets
+
+    def add_window(self, st: Stimulus, t_begin: int, t_end: int) -> int:
+        nets = np.ascontiguousarray(st.nets, np.uint32)
+        evs = np.ascontiguousarray(st.ev_start, np.uint64)
+        tm = np.ascontiguousarray(st.time, np.uint32)
+        vl = np.ascontiguousarray(st.value, np.uint8)
+        s = StimulusC(len(nets), _ptr(nets), _ptr(evs), _ptr(tm) if len(tm) else None,
+                      _ptr(vl) if len(vl) else None)
+        wid = C.c_uint32()
+        self._check(self.lib.gls_add_window(self.h, C.byref(s), t_begin, t_end, C.byref(wid)), "add_window")
+        return wid.value
+
+    def clear_windows(self):
+        self._check(self.lib.gls_clear_windows(self.h), "clear_windows")
+
+    def run(self):
+        self._check(self.lib.gls_run(self.h), "run")
+
+    def saif(self, window: int = 0) -> np.ndarray:
+        """(n_nets, 3) uint64: T0, T1, TX; UINT64_MAX rows were not produced."""
+        t0 = np.zeros(self.n_nets, np.uint64)
+        t1 = np.zeros(self.n_nets, np.uint64)
+        tx = np.zeros(self.n_nets, np.uint64)
+        self._check(self.lib.gls_saif_counts(self.h, window, _ptr(t0), _ptr(t1), _ptr(tx)), "saif_counts")
+        return np.stack([t0, t1, tx], axis=1)
+
+    def lengths(self, window: int = 0) -> np.ndarray:
+        ln = np.zeros(self.n_nets, np.uint32)
+        self._check(self.lib.gls_waveform_lengths(self.h, window, _ptr(ln)), "waveform_lengths")
+        return ln
+
+    def waveform(self, net: int, window: int = 0):
+        n = C.c_uint64()
+        self._check(self.lib.gls_waveform(self.h, window, net, None, None, 0, C.byref(n)), "waveform")
+        if n.value == 2**64 - 1:
+            return None
+        t = np.zeros(n.value, np.uint32)
+        v = np.zeros(n.value, np.uint8)
+        self._check(self.lib.gls_waveform(self.h, window, net, _ptr(t), _ptr(v), n.value, C.byref(n)), "waveform")
+        return t, v
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.gls_stats_get(self.h, C.byref(s)), "stats")
+        return s.as_dict()

@@ -1,0 +1,194 @@
+/*
+ * gls.h -- C ABI of the GB300 gate-level simulation library (libgls.so).
+ *
+ * The reference (YiwiSun/gate-level-simulator) exposes its simulate stage
+ * only as a CLI over files; its in-process boundary is the per-level host
+ * loop of src/simulate.cu:2027-3254, which stages each level's fan-in
+ * waveforms, launches the kernels of src/simulate.cu:486-1555 and writes
+ * SAIF through the DumpSaif overloads of src/simulate.cu:113-481.  The entry
+ * points below replace that loop; each cites the reference code it stands in
+ * for.  The simulation semantics are those of the reference's serial CPU
+ * simulator, src/simulate.cpp:872-1506.
+ *
+ * Conventions
+ *   - Every call returns an int status: GLS_OK (0) or a GLS_E* code; the
+ *     library never calls exit().  gls_last_error() gives a message.
+ *   - The context owns all device memory.  Host pointers passed in are only
+ *     read during the call.
+ *   - A context is used by one host thread at a time.
+ *   - Results do not depend on launch configuration or segment size.
+ *
+ * Value encoding (src/VCDTypes.h:49-54): 0 = logic 0, 1 = X, 2 = Z, 3 = 1.
+ * Times are unsigned 32-bit integers in the VCD time unit, as in the
+ * reference GPU tool (src/simulate.cu:2020-2023).
+ */
+#ifndef GLS_H
+#define GLS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLS_ABI_VERSION 1
+
+/* status codes */
+#define GLS_OK 0
+#define GLS_EINVAL 1      /* bad argument or malformed netlist / stimulus */
+#define GLS_ECUDA 2       /* CUDA runtime error */
+#define GLS_ENOMEM 3      /* device or host allocation failed */
+#define GLS_ESTATE 4      /* call out of order (e.g. run before load) */
+#define GLS_ERANGE 5      /* a time or size does not fit the 32-bit pool */
+#define GLS_EOVERFLOW 6   /* event pool exhausted and could not grow */
+
+/* calc modes: which gate-evaluation semantics the cell truth tables use */
+#define GLS_CALC_FIXED 0    /* 4-state Verilog primitives (Z reads as X) */
+#define GLS_CALC_LITERAL 1  /* the shipped calc of src/simulate.cpp:382-870 */
+
+/* output allocation modes */
+#define GLS_ALLOC_BOUND 0   /* slot per gate = sum of fan-in events + segments */
+#define GLS_ALLOC_EXACT 1   /* count in scratch, then copy to exact-size lists */
+
+/* primitive ids of the reference function program (src/PreProcess.cpp:1194-1197) */
+#define GLS_F_AND 0
+#define GLS_F_OR 1
+#define GLS_F_XOR 2
+#define GLS_F_XNOR 3
+#define GLS_F_NOR 4
+#define GLS_F_NAND 5
+#define GLS_F_BUF 6
+#define GLS_F_NOT 7
+#define GLS_F_UDP_XBUF 8
+#define GLS_F_UDP_MUX2 9
+/* pin codes inside a primitive (src/PreProcess.cpp:1199-1263): cell input k
+ * is k, cell output k is n_in + k, internal wires follow, and the supply
+ * nets are these two constants. */
+#define GLS_PIN_SUPPLY0 16
+#define GLS_PIN_SUPPLY1 17
+
+typedef struct gls_ctx gls_ctx;
+
+typedef struct {
+    int device;            /* CUDA device ordinal */
+    int calc_mode;         /* GLS_CALC_* */
+    int alloc_mode;        /* GLS_ALLOC_* */
+    double delay_factor;   /* SDF delay -> time unit factor; 1.0 for ps
+                              (src/simulate.cpp:1165-1175) */
+    uint32_t seg_events;   /* fan-in events per time segment (0 = default) */
+    uint64_t pool_events;  /* initial event-pool capacity (0 = automatic) */
+    void *stream;          /* cudaStream_t to launch on (NULL = own stream) */
+} gls_opts;
+
+/* One library cell: its primitive program in the reference encoding
+ * (Instance::function_id_vec, src/PreProcess.cpp:1194-1263). */
+typedef struct {
+    uint8_t n_in, n_out, n_prim, reserved;
+    uint32_t prim_start;   /* index of the first primitive in prims[] */
+} gls_cell;
+
+typedef struct {
+    uint8_t func;          /* GLS_F_* */
+    uint8_t n_pins;        /* inputs followed by the one driven pin */
+    uint8_t pins[14];
+} gls_prim;
+
+/* An SDF IOPATH arc (Delay, src/VCDTypes.h:166-186).  edge: 0 posedge,
+ * 1 negedge, 2 both.  Delays are in SDF units before delay_factor. */
+typedef struct {
+    uint8_t edge, in_pin, out_pin, reserved[5];
+    double rise, fall;
+} gls_arc;
+
+/* The levelized netlist, as `process` packs it into inter.dat
+ * (src/process.cpp:58-79, 252-566).  Instances are stored in level order. */
+typedef struct {
+    uint32_t n_nets;
+    uint32_t n_cells;
+    const gls_cell *cells;
+    uint32_t n_prims;
+    const gls_prim *prims;
+    uint32_t n_inst;
+    uint32_t n_levels;
+    const uint32_t *level_start;   /* n_levels + 1, into the instance arrays */
+    const uint32_t *inst_cell;     /* n_inst */
+    const uint32_t *inst_pin_start;/* n_inst + 1, into inst_pin_net */
+    const uint32_t *inst_pin_net;  /* per instance: n_in input nets, then n_out output nets */
+    const uint32_t *inst_arc_start;/* n_inst + 1, into arcs */
+    const gls_arc *arcs;
+} gls_netlist;
+
+/* Change-only waveforms of the nets the VCD drives (the per-signal time /
+ * value vectors of VCDParser, src/VCDParser.h:46-57), plus constant nets
+ * (a single event at time 0).  Times strictly increase within a net. */
+typedef struct {
+    uint32_t n_nets;
+    const uint32_t *net;           /* netlist net ids */
+    const uint64_t *ev_start;      /* n_nets + 1 */
+    const uint32_t *time;
+    const uint8_t *value;
+} gls_stimulus;
+
+typedef struct {
+    uint64_t gate_events;     /* sum over gate outputs of fan-in events */
+    uint64_t output_events;   /* events written to gate outputs */
+    uint64_t segments;        /* time segments simulated */
+    uint64_t pool_events;     /* event-pool capacity in use */
+    uint64_t pool_bytes;      /* device bytes held by the pool */
+    uint64_t overflow_retries;/* pool regrowths */
+    double kernel_ms;         /* device time of the last gls_run */
+    uint32_t launches;        /* kernels launched by the last gls_run */
+    uint32_t n_windows;
+} gls_stats;
+
+/* Create a context on opts->device.  Replaces cudaSetDevice(0) and the
+ * constant uploads of src/simulate.cu:1897-1957. */
+int gls_create(const gls_opts *opts, gls_ctx **out);
+int gls_destroy(gls_ctx *ctx);
+const char *gls_last_error(const gls_ctx *ctx);
+
+/* Copy the levelized netlist to the device and build per-gate truth tables
+ * and arc tables.  Replaces the archive load and the level-invariant uploads
+ * of src/simulate.cu:1835-1957 (inter.dat fields listed above). */
+int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl);
+
+/* Add a stimulus window (SAIF integral over [t_begin, t_end)).  Replaces
+ * VCDParser::parse/process and the per-level H2D staging of primary inputs
+ * (src/simulate.cu:1974-1989, 2166-2219, 2441-2477). */
+int gls_add_window(gls_ctx *ctx, const gls_stimulus *stim, uint64_t t_begin,
+                   uint64_t t_end, uint32_t *window_id);
+int gls_clear_windows(gls_ctx *ctx);
+
+/* Simulate every added window through all levels.  Replaces the per-level
+ * loop src/simulate.cu:2027-3254 (merge, SimulateCuda, compaction, D2H). */
+int gls_run(gls_ctx *ctx);
+
+/* T0 / T1 / TX per net for a window (arrays of n_nets).  Nets the run did
+ * not produce read UINT64_MAX.  Replaces the SAIF integrals of
+ * src/simulate.cu:174-253, 1592-1677 (serial: src/simulate.cpp:102-163). */
+int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint64_t *t1,
+                    uint64_t *tx);
+
+/* Number of events of every net (n_nets), UINT32_MAX where not produced. */
+int gls_waveform_lengths(gls_ctx *ctx, uint32_t window, uint32_t *len);
+
+/* One net's change list.  *n receives its length; up to cap events are
+ * copied.  Replaces the per-level D2H of src/simulate.cu:3207-3222. */
+int gls_waveform(gls_ctx *ctx, uint32_t window, uint32_t net, uint32_t *time,
+                 uint8_t *value, uint64_t cap, uint64_t *n);
+
+int gls_stats_get(gls_ctx *ctx, gls_stats *st);
+
+/* Host helper: the truth table of output `out` of a cell under calc_mode,
+ * 4^n_in entries indexed by sum(value[pin] << 2*pin).  Evaluates the
+ * primitive program like RunFunction, src/simulate.cpp:1203-1363. */
+int gls_cell_lut(const gls_cell *cell, const gls_prim *prims, int out,
+                 int calc_mode, uint8_t *lut, uint32_t lut_cap);
+
+int gls_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLS_H */

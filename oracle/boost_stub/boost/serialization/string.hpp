@@ -1,0 +1,2 @@
+// Empty stub (TEST INFRASTRUCTURE ONLY).
+#include "access.hpp"

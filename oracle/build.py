@@ -1,0 +1,84 @@
+"""TEST INFRASTRUCTURE ONLY: build the two CPU oracles.
+
+1. oracle/_build/gls_oracle -- the C restatement (oracle/gls_oracle.c).
+2. oracle/_ref/ref_sim      -- the reference's own serial simulator core.
+   Recipe: take src/simulate.cpp of the reference up to its `main` (which
+   does not compile against the shipped VCDParser), rename its `calc` so
+   oracle/ref_driver.cpp can choose the calc mode, and compile it with the
+   reference headers, empty Boost stubs (oracle/boost_stub) and the shim
+   header oracle/ref_shim/simulate.h.  The extracted sources are written to
+   oracle/_ref/src (git-ignored, never committed) so that a machine without
+   the reference checkout can rebuild the same binary.
+"""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+ORACLE = Path(__file__).resolve().parent
+BUILD = ORACLE / "_build"
+REF = ORACLE / "_ref"
+REF_SRC = REF / "src"
+REFERENCE = Path(os.environ.get("GLS_REFERENCE", "/root/reference"))
+REF_HEADERS = ["VCDTypes.h", "Function.h", "Instance.h", "PreProcess.h", "VCDValue.h"]
+
+ORACLE_BIN = BUILD / "gls_oracle"
+REF_BIN = REF / "ref_sim"
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"{' '.join(map(str, cmd))}\n{r.stdout}\n{r.stderr}")
+
+
+def build_oracle(force: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    src = ORACLE / "gls_oracle.c"
+    if force or not ORACLE_BIN.exists() or ORACLE_BIN.stat().st_mtime < src.stat().st_mtime:
+        _run(["gcc", "-O2", "-std=c11", "-pthread", "-o", str(ORACLE_BIN), str(src)])
+    return ORACLE_BIN
+
+
+def extract_reference() -> bool:
+    """Write oracle/_ref/src from the reference checkout; False if absent."""
+    sim = REFERENCE / "src" / "simulate.cpp"
+    if not sim.exists():
+        return False
+    REF_SRC.mkdir(parents=True, exist_ok=True)
+    text = sim.read_text()
+    cut = text.index("\nint main(")
+    core = text[:cut]
+    core, n = re.subn(r"\bvoid calc\(std::string name", "void gls_ref_calc_literal(std::string name", core)
+    if n != 1:
+        raise RuntimeError("reference calc definition not found")
+    (REF_SRC / "ref_core.cpp").write_text(core)
+    for h in REF_HEADERS:
+        shutil.copyfile(REFERENCE / "src" / h, REF_SRC / h)
+    return True
+
+
+def build_reference(force: bool = False) -> Path | None:
+    """Build oracle/_ref/ref_sim; None when no reference sources are present."""
+    have = extract_reference() or (REF_SRC / "ref_core.cpp").exists()
+    if not have:
+        return None
+    deps = [REF_SRC / "ref_core.cpp", ORACLE / "ref_driver.cpp", ORACLE / "ref_shim" / "simulate.h"]
+    if force or not REF_BIN.exists() or any(REF_BIN.stat().st_mtime < d.stat().st_mtime for d in deps):
+        # -DNDEBUG: the reference's asserts would abort on inputs its release
+        # behaviour handles (an X input edge is taken as posedge).
+        _run(["g++", "-O2", "-std=c++17", "-DNDEBUG", "-pthread", "-w",
+              f"-I{ORACLE / 'ref_shim'}", f"-I{ORACLE / 'boost_stub'}", f"-I{REF_SRC}",
+              "-o", str(REF_BIN), str(REF_SRC / "ref_core.cpp"), str(ORACLE / "ref_driver.cpp")])
+    return REF_BIN
+
+
+def build_all(force: bool = False):
+    return build_oracle(force), build_reference(force)
+
+
+if __name__ == "__main__":
+    print(build_all(force=True))
