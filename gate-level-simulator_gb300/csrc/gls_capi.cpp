@@ -42,13 +42,35 @@ struct DevBuf {
     template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+struct PinBuf {   // page-locked host staging, reused across windows
+    void *p = nullptr;
+    size_t bytes = 0;
+    bool ensure(size_t n)
+    {
+        if (n <= bytes && p) return true;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaHostAlloc(&p, n ? n : 16, cudaHostAllocDefault) != cudaSuccess) return false;
+        bytes = n ? n : 16;
+        return true;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
 struct Window {
     std::vector<uint32_t> stim_nets;
     std::vector<uint64_t> stim_off;     // aligned pool offset per stimulus net
     std::vector<uint32_t> stim_len;
     uint64_t stim_events = 0;           // aligned extent of the stimulus in the pool
-    std::vector<uint32_t> h_time;       // packed stimulus (kept to re-upload on pool growth)
-    std::vector<uint8_t> h_value;
+    PinBuf h_time, h_value;             // packed stimulus (kept to re-upload on pool growth)
+    PinBuf h_off, h_len;                // initial net table
     uint64_t t_begin = 0, t_end = 0;
     uint64_t cap = 0;
     DevBuf pool_t, pool_v, net_off, net_len, init_off, init_len, saif, small, stim_dev;
@@ -76,8 +98,11 @@ struct gls_ctx {
     uint32_t seg_cap = 0;
     uint32_t def_delay = 1;
     std::vector<Window *> windows;
+    std::vector<Window *> spare;     // cleared windows whose buffers are reused
     gls_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> prof;   // per-launch events when opts.profile
+    size_t prof_used = 0;
 };
 
 namespace {
@@ -159,6 +184,7 @@ static void free_window(Window *w)
     w->pool_t.release(); w->pool_v.release(); w->net_off.release(); w->net_len.release();
     w->init_off.release(); w->init_len.release(); w->saif.release(); w->small.release();
     w->stim_dev.release();
+    w->h_time.release(); w->h_value.release(); w->h_off.release(); w->h_len.release();
     delete w;
 }
 
@@ -167,7 +193,10 @@ extern "C" int gls_clear_windows(gls_ctx *ctx)
     if (!ctx) return GLS_EINVAL;
     cudaSetDevice(ctx->opts.device);
     cudaStreamSynchronize(ctx->stream);
-    for (Window *w : ctx->windows) free_window(w);
+    for (Window *w : ctx->windows) {
+        w->done = false;
+        ctx->spare.push_back(w);
+    }
     ctx->windows.clear();
     return GLS_OK;
 }
@@ -176,8 +205,11 @@ extern "C" int gls_destroy(gls_ctx *ctx)
 {
     if (!ctx) return GLS_EINVAL;
     gls_clear_windows(ctx);
+    for (Window *w : ctx->spare) free_window(w);
+    ctx->spare.clear();
     ctx->meta.release(); ctx->arcs.release(); ctx->lut.release();
     ctx->seg_base.release(); ctx->slot.release(); ctx->segs.release();
+    for (cudaEvent_t e : ctx->prof) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -328,19 +360,22 @@ static int upload_window(gls_ctx *ctx, Window *w)
     CK(w->small.ensure(256), "alloc counters");
     CK(w->stim_dev.ensure(w->stim_nets.size() * 4), "alloc stim nets");
     if (w->stim_events) {
-        CK(cudaMemcpyAsync(w->pool_t.p, w->h_time.data(), w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
+        CK(cudaMemcpyAsync(w->pool_t.p, w->h_time.p, w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
            "upload stimulus times");
-        CK(cudaMemcpyAsync(w->pool_v.p, w->h_value.data(), w->stim_events, cudaMemcpyHostToDevice, ctx->stream),
+        CK(cudaMemcpyAsync(w->pool_v.p, w->h_value.p, w->stim_events, cudaMemcpyHostToDevice, ctx->stream),
            "upload stimulus values");
     }
-    std::vector<uint64_t> off(n, 0);
-    std::vector<uint32_t> len(n, 0xFFFFFFFFu);
+    if (!w->h_off.ensure(n * 8) || !w->h_len.ensure(n * 4)) return fail(ctx, GLS_ENOMEM, "pinned staging");
+    uint64_t *off = w->h_off.as<uint64_t>();
+    uint32_t *len = w->h_len.as<uint32_t>();
+    std::memset(off, 0, n * 8);
+    std::memset(len, 0xFF, n * 4);
     for (size_t k = 0; k < w->stim_nets.size(); ++k) {
         off[w->stim_nets[k]] = w->stim_off[k];
         len[w->stim_nets[k]] = w->stim_len[k];
     }
-    CK(cudaMemcpyAsync(w->init_off.p, off.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream), "upload offsets");
-    CK(cudaMemcpyAsync(w->init_len.p, len.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream), "upload lengths");
+    CK(cudaMemcpyAsync(w->init_off.p, off, n * 8, cudaMemcpyHostToDevice, ctx->stream), "upload offsets");
+    CK(cudaMemcpyAsync(w->init_len.p, len, n * 4, cudaMemcpyHostToDevice, ctx->stream), "upload lengths");
     if (!w->stim_nets.empty())
         CK(cudaMemcpyAsync(w->stim_dev.p, w->stim_nets.data(), w->stim_nets.size() * 4, cudaMemcpyHostToDevice,
                            ctx->stream),
@@ -359,24 +394,31 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     if (st->n_nets && (!st->net || !st->ev_start || !st->time || !st->value))
         return fail(ctx, GLS_EINVAL, "stimulus: null array");
     cudaSetDevice(ctx->opts.device);
-    Window *w = new Window();
+    Window *w;
+    if (!ctx->spare.empty()) {
+        w = ctx->spare.back();
+        ctx->spare.pop_back();
+    } else {
+        w = new Window();
+    }
+    w->done = false;
     w->t_begin = t_begin;
     w->t_end = t_end;
     std::vector<uint8_t> seen(ctx->n_nets, 0);
     uint64_t total = 0, maxlen = 0;
     for (uint32_t k = 0; k < st->n_nets; ++k) {
         const uint32_t net = st->net[k];
-        if (net >= ctx->n_nets) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u out of range", net); }
-        if (seen[net]) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u given twice", net); }
-        if (ctx->driven[net]) { delete w; return fail(ctx, GLS_EINVAL, "stimulus net %u is driven by a gate", net); }
+        if (net >= ctx->n_nets) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u out of range", net); }
+        if (seen[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u given twice", net); }
+        if (ctx->driven[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u is driven by a gate", net); }
         seen[net] = 1;
         const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
-        if (b < a) { delete w; return fail(ctx, GLS_EINVAL, "stimulus ev_start not monotone"); }
+        if (b < a) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus ev_start not monotone"); }
         for (uint64_t e = a; e < b; ++e) {
-            if (st->value[e] > 3) { delete w; return fail(ctx, GLS_EINVAL, "stimulus value %u", st->value[e]); }
-            if (st->time[e] == 0xFFFFFFFFu) { delete w; return fail(ctx, GLS_ERANGE, "stimulus time 2^32-1"); }
+            if (st->value[e] > 3) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus value %u", st->value[e]); }
+            if (st->time[e] == 0xFFFFFFFFu) { ctx->spare.push_back(w); return fail(ctx, GLS_ERANGE, "stimulus time 2^32-1"); }
             if (e > a && st->time[e] <= st->time[e - 1]) {
-                delete w;
+                ctx->spare.push_back(w);
                 return fail(ctx, GLS_EINVAL, "stimulus net %u: times not strictly increasing", net);
             }
         }
@@ -384,21 +426,27 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         maxlen = std::max<uint64_t>(maxlen, b - a);
     }
     for (uint32_t net : ctx->ext_inputs)
-        if (!seen[net]) { delete w; return fail(ctx, GLS_EINVAL, "net %u is read by a gate but has no stimulus", net); }
+        if (!seen[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "net %u is read by a gate but has no stimulus", net); }
     // pack the stimulus into the pool layout (each net on a 4-event boundary)
     w->stim_nets.assign(st->net, st->net + st->n_nets);
     w->stim_off.resize(st->n_nets);
     w->stim_len.resize(st->n_nets);
-    w->h_time.assign(total, 0);
-    w->h_value.assign(total, kVX);
+    if (!w->h_time.ensure(total * 4) || !w->h_value.ensure(total)) {
+        ctx->spare.push_back(w);
+        return fail(ctx, GLS_ENOMEM, "pinned staging of %llu events", (unsigned long long)total);
+    }
     uint64_t at = 0;
     for (uint32_t k = 0; k < st->n_nets; ++k) {
         const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
         w->stim_off[k] = at;
         w->stim_len[k] = (uint32_t)(b - a);
         if (b > a) {
-            std::memcpy(w->h_time.data() + at, st->time + a, (b - a) * 4);
-            std::memcpy(w->h_value.data() + at, st->value + a, b - a);
+            std::memcpy(w->h_time.as<uint32_t>() + at, st->time + a, (b - a) * 4);
+            std::memcpy(w->h_value.as<uint8_t>() + at, st->value + a, b - a);
+        }
+        for (uint64_t e = b - a; e < round4(b - a); ++e) {
+            w->h_time.as<uint32_t>()[at + e] = 0;
+            w->h_value.as<uint8_t>()[at + e] = kVX;
         }
         at += round4(b - a);
     }
@@ -414,7 +462,7 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
             if (cap > limit) cap = std::max<uint64_t>(limit, total + 1024);
         }
     }
-    w->cap = std::max<uint64_t>(cap, total + 1024);
+    w->cap = std::max<uint64_t>(std::max<uint64_t>(cap, total + 1024), w->cap);
     int rc = upload_window(ctx, w);
     if (rc) { free_window(w); return rc; }
     ctx->windows.push_back(w);
@@ -432,9 +480,9 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     d.saif = w->saif.as<unsigned long long>();
     unsigned long long *sm = w->small.as<unsigned long long>();
     d.top = sm;
-    d.counters = sm + 1;     // 3 counters
-    d.err = reinterpret_cast<uint32_t *>(sm + 4);
-    d.n_segs = reinterpret_cast<uint32_t *>(sm + 5);
+    d.counters = sm + 1;     // 4 counters
+    d.err = reinterpret_cast<uint32_t *>(sm + 5);
+    d.n_segs = reinterpret_cast<uint32_t *>(sm + 6);
     d.seg_base = ctx->seg_base.as<uint32_t>();
     d.slot = ctx->slot.as<uint64_t>();
     d.segs = ctx->segs.as<SegRec>();
@@ -443,6 +491,24 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     d.t_begin = w->t_begin;
     d.t_end = w->t_end;
     return d;
+}
+
+// profiling: events recorded between kernel launches (opts.profile)
+static cudaEvent_t prof_event(gls_ctx *ctx)
+{
+    if (ctx->prof_used == ctx->prof.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ctx->prof.push_back(e);
+    }
+    return ctx->prof[ctx->prof_used++];
+}
+
+static void prof_mark(gls_ctx *ctx)
+{
+    if (!ctx->opts.profile) return;
+    cudaEvent_t e = prof_event(ctx);
+    if (e) cudaEventRecord(e, ctx->stream);
 }
 
 static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
@@ -454,8 +520,10 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     unsigned long long small[8] = {w->stim_events, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(w->small.p, small, sizeof small, cudaMemcpyHostToDevice, ctx->stream), "reset counters");
     WinDev d = make_windev(ctx, w);
+    prof_mark(ctx);
     launch_stim_saif(d, w->stim_dev.as<uint32_t>(), (uint32_t)w->stim_nets.size(), ctx->stream);
     ++*launches;
+    prof_mark(ctx);
     LevelArgs a;
     a.meta = ctx->meta.as<DrvMeta>();
     a.arcs = ctx->arcs.as<ArcDev>();
@@ -465,7 +533,14 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
         a.lo = ctx->drv_level_start[L];
         a.hi = ctx->drv_level_start[L + 1];
-        launch_level(d, a, ctx->sm_count, ctx->stream, launches);
+        if (a.hi == a.lo) continue;
+        launch_plan(d, a, ctx->stream);
+        prof_mark(ctx);
+        launch_sim(d, a, ctx->sm_count, ctx->stream);
+        prof_mark(ctx);
+        launch_combine(d, a, ctx->stream);
+        prof_mark(ctx);
+        *launches += 3;
     }
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;
@@ -477,6 +552,7 @@ extern "C" int gls_run(gls_ctx *ctx)
     if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "run before load_netlist");
     cudaSetDevice(ctx->opts.device);
     uint32_t launches = 0;
+    ctx->prof_used = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
     for (Window *w : ctx->windows) {
         int rc = enqueue_window(ctx, w, &launches);
@@ -487,17 +563,40 @@ extern "C" int gls_run(gls_ctx *ctx)
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     double total_ms = ms;
-    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0;
+    double kms[4] = {0, 0, 0, 0};   // stim, plan, sim, combine
+    if (ctx->opts.profile) {
+        // per window: [stim start, stim end, then per level: after plan, after sim, after combine]
+        size_t k = 0;
+        const size_t nlev = ctx->drv_level_start.size() - 1;
+        for (size_t wi = 0; wi < ctx->windows.size() && k + 1 < ctx->prof_used; ++wi) {
+            float x = 0.f;
+            cudaEventElapsedTime(&x, ctx->prof[k], ctx->prof[k + 1]);
+            kms[0] += x;
+            cudaEvent_t prev = ctx->prof[k + 1];
+            k += 2;
+            for (size_t L = 0; L < nlev; ++L) {
+                if (ctx->drv_level_start[L + 1] == ctx->drv_level_start[L]) continue;
+                if (k + 2 >= ctx->prof_used) break;
+                cudaEventElapsedTime(&x, prev, ctx->prof[k]); kms[1] += x;
+                cudaEventElapsedTime(&x, ctx->prof[k], ctx->prof[k + 1]); kms[2] += x;
+                cudaEventElapsedTime(&x, ctx->prof[k + 1], ctx->prof[k + 2]); kms[3] += x;
+                prev = ctx->prof[k + 2];
+                k += 3;
+            }
+        }
+    }
+    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0;
     // check every window; regrow the pool or the segment table and rerun
     for (Window *w : ctx->windows) {
         for (int attempt = 0;; ++attempt) {
             unsigned long long small[8];
             CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
-            const uint32_t err = (uint32_t)small[4];
+            const uint32_t err = (uint32_t)small[5];
             if (!err) {
                 gate_ev += small[1];
                 out_ev += small[2];
                 segs += small[3];
+                fanin_ev += small[4];
                 pool_ev += small[0];
                 pool_bytes += w->cap * 5;
                 break;
@@ -524,6 +623,7 @@ extern "C" int gls_run(gls_ctx *ctx)
                 ctx->stats.overflow_retries++;
             }
             uint32_t l2 = 0;
+            ctx->prof_used = 0;   // per-kernel times then cover the successful run only
             CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
             int rc = enqueue_window(ctx, w, &l2);
             if (rc) return rc;
@@ -543,6 +643,11 @@ extern "C" int gls_run(gls_ctx *ctx)
     ctx->stats.kernel_ms = total_ms;
     ctx->stats.launches = launches;
     ctx->stats.n_windows = (uint32_t)ctx->windows.size();
+    ctx->stats.stim_ms = kms[0];
+    ctx->stats.plan_ms = kms[1];
+    ctx->stats.sim_ms = kms[2];
+    ctx->stats.combine_ms = kms[3];
+    ctx->stats.fanin_bytes = fanin_ev * 5;
     return GLS_OK;
 }
 

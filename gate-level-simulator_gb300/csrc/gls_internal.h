@@ -55,7 +55,7 @@ struct WinDev {
     uint8_t *pool_v;
     unsigned long long *saif;   // 3 per net
     unsigned long long *top;    // pool bump pointer (events)
-    unsigned long long *counters;  // [0] gate events, [1] output events, [2] segments
+    unsigned long long *counters;  // [0] gate events, [1] output events, [2] segments, [3] fan-in events
     uint32_t *err;
     uint32_t *seg_base;         // per driver of the level, +1
     uint64_t *slot;             // per driver of the level: slot start in the pool
@@ -76,6 +76,8 @@ struct LevelArgs {
 };
 
 void launch_stim_saif(const WinDev &w, const uint32_t *stim_nets, uint32_t n_stim, cudaStream_t st);
-void launch_level(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st, uint32_t *launches);
+void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st);
+void launch_sim(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st);
+void launch_combine(const WinDev &w, const LevelArgs &a, cudaStream_t st);
 
 }  // namespace gls

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
         s_seg = seg;
         s_base = *w.top;
         atomicAdd(&w.counters[0], g_tot);
+        atomicAdd(&w.counters[3], e_tot);
     }
     __syncthreads();
     if (*w.err) return;
@@ -503,15 +504,21 @@ void launch_stim_saif(const WinDev &w, const uint32_t *stim_nets, uint32_t n_sti
     k_stim_saif<<<blocks, 256, 0, st>>>(w, stim_nets, n_stim);
 }
 
-void launch_level(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st, uint32_t *launches)
+void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st)
+{
+    k_plan<<<1, 1024, 0, st>>>(w, a);
+}
+
+void launch_sim(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st)
+{
+    k_sim<<<sm_count * 16, 128, 0, st>>>(w, a);
+}
+
+void launch_combine(const WinDev &w, const LevelArgs &a, cudaStream_t st)
 {
     const uint32_t n = a.hi - a.lo;
-    if (!n) return;
-    k_plan<<<1, 1024, 0, st>>>(w, a);
-    k_sim<<<sm_count * 16, 128, 0, st>>>(w, a);
     const uint32_t blocks = (uint32_t)(((uint64_t)n * 32 + 255) / 256);
     k_combine<<<blocks, 256, 0, st>>>(w, a);
-    *launches += 3;
 }
 
 }  // namespace gls

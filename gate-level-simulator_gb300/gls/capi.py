@@ -35,7 +35,7 @@ class GlsError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("device", C.c_int), ("calc_mode", C.c_int), ("alloc_mode", C.c_int),
                 ("delay_factor", C.c_double), ("seg_events", C.c_uint32), ("pool_events", C.c_uint64),
-                ("stream", C.c_void_p)]
+                ("stream", C.c_void_p), ("profile", C.c_int)]
 
 
 class NetlistC(C.Structure):
@@ -54,7 +54,9 @@ class StimulusC(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("gate_events", C.c_uint64), ("output_events", C.c_uint64), ("segments", C.c_uint64),
                 ("pool_events", C.c_uint64), ("pool_bytes", C.c_uint64), ("overflow_retries", C.c_uint64),
-                ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("n_windows", C.c_uint32)]
+                ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("n_windows", C.c_uint32),
+                ("plan_ms", C.c_double), ("sim_ms", C.c_double), ("combine_ms", C.c_double),
+                ("stim_ms", C.c_double), ("fanin_bytes", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -99,10 +101,13 @@ def _ptr(a: np.ndarray):
 
 def cell_lut(cell_rec: np.ndarray, prims: np.ndarray, out: int, calc_mode: int) -> np.ndarray:
     """Truth table of one cell output (host helper, no GPU needed)."""
+    from .netlist import CELL_DTYPE
+
     lib = load_library()
-    rec = np.ascontiguousarray(cell_rec.copy())
+    rec = np.zeros(1, CELL_DTYPE)
+    rec[0] = cell_rec
     rec["prim_start"] = 0
-    n = 1 << (2 * int(rec["n_in"]))
+    n = 1 << (2 * int(rec["n_in"][0]))
     lut = np.zeros(n, np.uint8)
     rc = lib.gls_cell_lut(_ptr(rec), _ptr(np.ascontiguousarray(prims)), out, calc_mode, _ptr(lut), n)
     if rc:
@@ -115,9 +120,10 @@ class Simulator:
 
     def __init__(self, device: int = 0, calc_mode: int = CALC_FIXED, seg_events: int = 0,
                  pool_events: int = 0, delay_factor: float = 1.0, stream: int | None = None,
-                 alloc_mode: int = ALLOC_BOUND):
+                 alloc_mode: int = ALLOC_BOUND, profile: bool = False):
         self.lib = load_library()
-        o = Opts(device, calc_mode, alloc_mode, delay_factor, seg_events, pool_events, stream or None)
+        o = Opts(device, calc_mode, alloc_mode, delay_factor, seg_events, pool_events, stream or None,
+                 1 if profile else 0)
         h = C.c_void_p()
         rc = self.lib.gls_create(C.byref(o), C.byref(h))
         if rc:

@@ -78,6 +78,7 @@ typedef struct {
     uint32_t seg_events;   /* fan-in events per time segment (0 = default) */
     uint64_t pool_events;  /* initial event-pool capacity (0 = automatic) */
     void *stream;          /* cudaStream_t to launch on (NULL = own stream) */
+    int profile;           /* 1: time every kernel class with CUDA events */
 } gls_opts;
 
 /* One library cell: its primitive program in the reference encoding
@@ -139,6 +140,9 @@ typedef struct {
     double kernel_ms;         /* device time of the last gls_run */
     uint32_t launches;        /* kernels launched by the last gls_run */
     uint32_t n_windows;
+    /* with opts.profile: device time per kernel class in the last gls_run */
+    double plan_ms, sim_ms, combine_ms, stim_ms;
+    uint64_t fanin_bytes;     /* fan-in event bytes the gate kernels read (5 B per event per net) */
 } gls_stats;
 
 /* Create a context on opts->device.  Replaces cudaSetDevice(0) and the

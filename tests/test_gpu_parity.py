@@ -1,0 +1,143 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden vectors, bit-exact on every waveform and SAIF count."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cases import random_case, stimulus
+from gls import synth
+from gls.capi import CALC_FIXED, CALC_LITERAL, GlsError, Simulator
+from gls.levelize import assemble
+from gpu_util import assert_same, gpu_run, waveform_properties
+from oracle.runner import run_oracle
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def golden_cases():
+    return json.loads((GOLD / "cases.json").read_text())
+
+
+@pytest.mark.parametrize("seg", [8, 0])
+@pytest.mark.parametrize("idx", range(len(golden_cases())))
+def test_gpu_matches_golden(idx, seg, gpu):
+    r = golden_cases()[idx]
+    insts = [(c, ins, outs, [tuple(a) for a in arcs]) for c, ins, outs, arcs in r["instances"]]
+    nl = assemble(insts, n_nets=r["n_nets"])
+    st = stimulus({int(k): [tuple(e) for e in v] for k, v in r["stimulus"].items()})
+    calc = CALC_LITERAL if r["calc"] == "literal" else CALC_FIXED
+    gw, gs, _, _ = gpu_run(nl, st, *r["window"], calc=calc, seg=seg)
+    for net, ev in r["waves"].items():
+        exp = np.array(ev, np.int64).reshape(-1, 2)
+        t, v = gw[int(net)]
+        assert np.array_equal(t.astype(np.int64), exp[:, 0]) and np.array_equal(v.astype(np.int64), exp[:, 1]), \
+            f"{r['label']}: net {net}"
+    for net, rec in r["saif"].items():
+        assert gs[int(net)].tolist() == rec, f"{r['label']}: SAIF net {net}"
+
+
+@pytest.mark.parametrize("seg", [8, 13, 256])
+@pytest.mark.parametrize("seed", range(16))
+def test_gpu_random_vs_oracle(seed, seg, gpu, oracle_bin):
+    nl, st = random_case(seed, max_gates=16, max_in=6, horizon=600, max_events=80,
+                         zero_delay=(seed % 5 == 0))
+    calc = "literal" if seed % 4 == 3 else "fixed"
+    try:
+        ow, osaif, _ = run_oracle(nl, st, 0, 700, calc=calc)
+    except Exception:
+        pytest.skip("oracle rejects this case (zero delay at time 0)")
+    gw, gs, _, _ = gpu_run(nl, st, 0, 700, calc=CALC_LITERAL if calc == "literal" else CALC_FIXED, seg=seg)
+    assert_same(gw, gs, ow, osaif, f"seed {seed} seg {seg}")
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_gpu_dense_random_vs_oracle(seed, gpu, oracle_bin):
+    """Many gates and long lists: every level has several segments per gate."""
+    nl, st = random_case(900 + seed, max_gates=120, max_in=8, horizon=20000, max_events=2000, xz=seed % 2 == 0)
+    ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
+    for seg in (16, 512):
+        gw, gs, _, _ = gpu_run(nl, st, 100, 15000, seg=seg)
+        assert_same(gw, gs, ow, osaif, f"dense seed {seed} seg {seg}")
+
+
+def test_gpu_c1_full_config(gpu, oracle_bin):
+    """The small benchmark configuration end to end: 2,000 cells, depth 20,
+    192 pseudo-primary inputs, 1,000 cycles, window 0..1,000,000 ps."""
+    cfg = synth.CONFIGS["c1"]
+    nl = synth.make_netlist(cfg, seed=1)
+    st = synth.make_stimulus(cfg, nl.ppi_nets, seed=2)
+    ow, osaif, _ = run_oracle(nl, st, 0, cfg.t_end, threads=8)
+    gw, gs, _, stats = gpu_run(nl, st, 0, cfg.t_end)
+    assert_same(gw, gs, ow, osaif, "c1")
+    assert stats["gate_events"] > 0 and stats["output_events"] > 0
+
+
+def test_gpu_c2_shape_scaled(gpu, oracle_bin):
+    """The medium configuration's generator at 20,000 cells and 1,500 cycles."""
+    cfg = synth.scaled(synth.CONFIGS["c2"], cells=20_000, cycles=1_500)
+    nl = synth.make_netlist(cfg, seed=3)
+    st = synth.make_stimulus(cfg, nl.ppi_nets, seed=4)
+    ow, osaif, _ = run_oracle(nl, st, 0, cfg.t_end, threads=16)
+    gw, gs, _, _ = gpu_run(nl, st, 0, cfg.t_end)
+    assert_same(gw, gs, ow, osaif, "c2-scaled")
+
+
+def test_gpu_segment_size_invariance_and_properties(gpu):
+    cfg = synth.scaled(synth.CONFIGS["c3"], cells=30_000, cycles=3_000, depth=40, ppi=2048)
+    nl = synth.make_netlist(cfg, seed=5)
+    st = synth.make_stimulus(cfg, nl.ppi_nets, seed=6)
+    driven = set(nl.gate_output_nets().tolist())
+    a = gpu_run(nl, st, 0, cfg.t_end, seg=32)
+    b = gpu_run(nl, st, 0, cfg.t_end, seg=4096)
+    assert np.array_equal(a[2], b[2]) and np.array_equal(a[1], b[1])
+    for n in a[0]:
+        assert np.array_equal(a[0][n][0], b[0][n][0]) and np.array_equal(a[0][n][1], b[0][n][1])
+    waveform_properties(a[0], a[1], 0, cfg.t_end, driven)
+
+
+def test_gpu_window_inside_activity(gpu, oracle_bin):
+    nl, st = random_case(31, max_gates=30, max_in=5, horizon=5000, max_events=300)
+    for tb, te in [(1000, 1001), (1234, 4321), (0, 1), (4999, 9000)]:
+        ow, osaif, _ = run_oracle(nl, st, tb, te)
+        gw, gs, _, _ = gpu_run(nl, st, tb, te)
+        assert_same(gw, gs, ow, osaif, f"window {tb}..{te}")
+
+
+def test_gpu_empty_and_constant_inputs(gpu, oracle_bin):
+    # net 0 has no events at all (reads X), net 1 is a constant, net 2 toggles
+    nl = assemble([("GEN_AND2_D1", [0, 2], [3], [(2, "a1", "z", 5, 7), (2, "a2", "z", 9, 11)]),
+                   ("GEN_OR2_D1", [1, 2], [4], [(2, "a1", "z", 5, 7), (2, "a2", "z", 9, 11)]),
+                   ("GEN_MUX2_D1", [3, 4, 1], [5], [(2, "i0", "z", 3, 4), (2, "i1", "z", 5, 6),
+                                                   (0, "s", "z", 7, 8), (1, "s", "z", 9, 10)])])
+    st = stimulus({0: [], 1: [(0, 3)], 2: [(0, 0), (100, 3), (105, 0), (300, 3)]})
+    ow, osaif, _ = run_oracle(nl, st, 0, 1000)
+    gw, gs, _, _ = gpu_run(nl, st, 0, 1000)
+    assert_same(gw, gs, ow, osaif, "empty/constant")
+
+
+def test_gpu_rejects_bad_input(gpu):
+    nl = assemble([("GEN_INV_D1", [0], [1], [(2, "i", "zn", 5, 5)])])
+    with Simulator() as s:
+        s.load(nl)
+        with pytest.raises(GlsError):          # read net 0 has no stimulus
+            s.add_window(stimulus({}), 0, 10)
+        with pytest.raises(GlsError):          # times must strictly increase
+            s.add_window(stimulus({0: [(0, 0), (5, 3), (5, 0)]}), 0, 10)
+        with pytest.raises(GlsError):          # the stimulus cannot drive a gate output
+            s.add_window(stimulus({0: [(0, 0)], 1: [(0, 0)]}), 0, 10)
+        with pytest.raises(GlsError):          # empty window
+            s.add_window(stimulus({0: [(0, 0)]}), 10, 10)
+        with pytest.raises(GlsError):          # not simulated yet
+            s.saif(0)
+
+
+def test_gpu_pool_regrowth(gpu, oracle_bin):
+    """A deliberately tiny initial event pool must grow and give the same result."""
+    nl, st = random_case(44, max_gates=40, max_in=4, horizon=4000, max_events=400)
+    ow, osaif, _ = run_oracle(nl, st, 0, 4000)
+    gw, gs, _, stats = gpu_run(nl, st, 0, 4000, pool_events=64)
+    assert stats["overflow_retries"] >= 1
+    assert_same(gw, gs, ow, osaif, "regrowth")
