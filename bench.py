@@ -39,6 +39,14 @@ WORKLOADS = {
 }
 
 
+def workload_desc(args) -> str:
+    base = WORKLOADS[args.config]
+    if args.cells or args.depth or args.cycles:
+        return (f"{args.config} generator scaled: cells={args.cells or 'default'}, depth={args.depth or 'default'}, "
+                f"cycles={args.cycles or 'default'} (profiling case, not the benchmark workload)")
+    return base
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -96,9 +104,11 @@ def peak_hbm():
     return 6800.0, "fallback"
 
 
-def make_workload(name: str, seed: int):
+def make_workload(name: str, seed: int, cells=None, depth=None, cycles=None):
     from gls import synth
     cfg = synth.CONFIGS[name]
+    if cells or depth or cycles:
+        cfg = synth.scaled(cfg, cells=cells, depth=depth, cycles=cycles)
     t0 = time.time()
     nl = synth.make_netlist(cfg, seed=seed)
     log(f"netlist {name}: {nl.n_inst} cells, {nl.n_levels} levels ({time.time() - t0:.1f}s)")
@@ -176,7 +186,7 @@ def reference_arm(args):
     if rank != 0:
         return
     from oracle.runner import run_oracle
-    cfg, nl = make_workload(args.config, args.seed)
+    cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
     st = stimulus_for(cfg, nl, args.seed + 1)
     threads = os.cpu_count() or 1
     t0 = time.time()
@@ -196,7 +206,7 @@ def reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.config], "seed": args.seed},
+        "config": {"workload": workload_desc(args), "seed": args.seed},
         "cpu_baseline": {"value": v, "unit": "gate-events/s", "cores": threads, "kind": kind, "sample": desc},
         "e2e": {"value": v, "unit": "gate-events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -216,7 +226,7 @@ def gls_arm(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
-    cfg, nl = make_workload(args.config, args.seed)
+    cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
     # replicas: every rank simulates its own independent window (weak scaling)
     st = stimulus_for(cfg, nl, args.seed + 1 + 1000 * rank)
     sim = Simulator(device=local, stream=stream.cuda_stream, profile=True, seg_events=args.seg)
@@ -304,7 +314,7 @@ def gls_arm(args):
         "metric": "gate-events/s", "value": value, "unit": "gate-events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.config], "seed": args.seed, "parallelism": f"replicas x{world}",
+        "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
                    "seg_events": args.seg or 256},
         "sim_cycles_per_s": sim_cycles,
@@ -352,6 +362,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--seg", type=int, default=0, help="fan-in events per time segment (0 = library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling cases)")
+    ap.add_argument("--depth", type=int, default=None, help="override the logic depth (profiling cases)")
+    ap.add_argument("--cycles", type=int, default=None, help="override the cycle count (profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

@@ -10,7 +10,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <map>
+#include <thread>
 #include <string>
 #include <vector>
 #include "gls.h"
@@ -69,11 +71,11 @@ struct Window {
     std::vector<uint64_t> stim_off;     // aligned pool offset per stimulus net
     std::vector<uint32_t> stim_len;
     uint64_t stim_events = 0;           // aligned extent of the stimulus in the pool
-    PinBuf h_time, h_value;             // packed stimulus (kept to re-upload on pool growth)
+    PinBuf h_words;                     // packed stimulus events (kept to re-upload on pool growth)
     PinBuf h_off, h_len;                // initial net table
     uint64_t t_begin = 0, t_end = 0;
     uint64_t cap = 0;
-    DevBuf pool_t, pool_v, net_off, net_len, init_off, init_len, saif, small, stim_dev;
+    DevBuf pool, net_off, net_len, init_off, init_len, saif, small, stim_dev;
     bool done = false;
 };
 
@@ -89,13 +91,15 @@ struct gls_ctx {
     uint32_t n_nets = 0;
     uint32_t n_drv = 0;
     std::vector<uint32_t> drv_level_start;   // per level, into drivers
+    std::vector<uint32_t> cls_start;         // per level kClasses+1 entries: fan-in class ranges, level-relative
     uint32_t max_width = 0;
     uint64_t pins_total = 0;
     std::vector<uint8_t> driven;             // net driven by a gate output
     std::vector<uint32_t> ext_inputs;        // nets read by gates and driven by no gate
-    DevBuf meta, arcs, lut;
-    DevBuf seg_base, slot, segs;
+    DevBuf meta, arcs, ndel, lut;
+    DevBuf seg_base, slot, scr, segs, copies, scratch;
     uint32_t seg_cap = 0;
+    uint64_t scr_cap = 0;
     uint32_t def_delay = 1;
     std::vector<Window *> windows;
     std::vector<Window *> spare;     // cleared windows whose buffers are reused
@@ -152,7 +156,6 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         delete ctx;
         return GLS_EINVAL;
     }
-    if (!ctx->opts.seg_events) ctx->opts.seg_events = 256;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0 || ctx->opts.device < 0 || ctx->opts.device >= ndev) {
@@ -181,10 +184,10 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
 
 static void free_window(Window *w)
 {
-    w->pool_t.release(); w->pool_v.release(); w->net_off.release(); w->net_len.release();
+    w->pool.release(); w->net_off.release(); w->net_len.release();
     w->init_off.release(); w->init_len.release(); w->saif.release(); w->small.release();
     w->stim_dev.release();
-    w->h_time.release(); w->h_value.release(); w->h_off.release(); w->h_len.release();
+    w->h_words.release(); w->h_off.release(); w->h_len.release();
     delete w;
 }
 
@@ -207,8 +210,10 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     gls_clear_windows(ctx);
     for (Window *w : ctx->spare) free_window(w);
     ctx->spare.clear();
-    ctx->meta.release(); ctx->arcs.release(); ctx->lut.release();
-    ctx->seg_base.release(); ctx->slot.release(); ctx->segs.release();
+    ctx->meta.release(); ctx->arcs.release(); ctx->ndel.release(); ctx->lut.release();
+    ctx->copies.release();
+    ctx->seg_base.release(); ctx->slot.release(); ctx->scr.release(); ctx->segs.release();
+    ctx->scratch.release();
     for (cudaEvent_t e : ctx->prof) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -236,8 +241,10 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     std::vector<uint8_t> h_lut;
     std::vector<DrvMeta> h_meta;
     std::vector<ArcDev> h_arcs;
+    std::vector<NetDelay> h_ndel;
     std::vector<int32_t> drv_level_of_net(nl->n_nets, -1);
     ctx->drv_level_start.assign(1, 0);
+    ctx->cls_start.clear();
     ctx->pins_total = 0;
     std::vector<uint8_t> consumed(nl->n_nets, 0);
     for (uint32_t L = 0; L < nl->n_levels; ++L) {
@@ -272,7 +279,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
             }
             md.m = (uint8_t)m;
             md.n_pins = cl.n_in;
-            md.ident = ident ? 1 : 0;
+            md.flags = ident ? kFlagIdent : 0;
             ctx->pins_total += cl.n_in;
             for (int o = 0; o < cl.n_out; ++o) {
                 DrvMeta d = md;
@@ -281,7 +288,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
                 if (drv_level_of_net[onet] >= 0) return fail(ctx, GLS_EINVAL, "net %u has two drivers", onet);
                 drv_level_of_net[onet] = (int32_t)L;
                 d.out_net = onet;
-                d.reserved = o == 0 ? 1u : 0u;
+                if (o == 0) d.flags |= kFlagFirstOut;
                 auto key = std::make_pair(cid, o);
                 auto it = lut_of.find(key);
                 if (it == lut_of.end()) {
@@ -314,9 +321,56 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
                 }
                 if (na > 255) return fail(ctx, GLS_EINVAL, "instance %u: too many arcs", i);
                 d.n_arcs = (uint8_t)na;
+                // per-net delay table when every net's arcs are regular
+                bool regular = true;
+                NetDelay nd[kMaxSlots];
+                for (int j = 0; j < m; ++j) {
+                    uint32_t rf[2][2] = {{kInf, kInf}, {kInf, kInf}};   // [edge][rise/fall]
+                    int nboth = 0, npos = 0, nneg = 0;
+                    for (uint32_t k = 0; k < na; ++k) {
+                        const ArcDev &A = h_arcs[d.arc_off + k];
+                        if ((int)(A.info >> 2) != j) continue;
+                        const int edge = A.info & 3u;
+                        if (edge == 2) {
+                            ++nboth;
+                            rf[0][0] = rf[1][0] = A.rise;
+                            rf[0][1] = rf[1][1] = A.fall;
+                        } else {
+                            ++(edge == 0 ? npos : nneg);
+                            rf[edge][0] = A.rise;
+                            rf[edge][1] = A.fall;
+                        }
+                    }
+                    const bool ok = (nboth == 0 && npos == 0 && nneg == 0) || (nboth == 1 && npos == 0 && nneg == 0) ||
+                                    (nboth == 0 && npos == 1 && nneg == 1);
+                    if (!ok) regular = false;
+                    for (int e = 0; e < 2; ++e) {
+                        const uint32_t r = rf[e][0], f = rf[e][1];
+                        nd[j].d[e * 4 + 0] = r;
+                        nd[j].d[e * 4 + 1] = f;
+                        nd[j].d[e * 4 + 2] = std::max(r, f);
+                        nd[j].d[e * 4 + 3] = std::min(r, f);
+                    }
+                }
+                d.dt_off = (uint32_t)h_ndel.size();
+                if (regular) {
+                    d.flags |= kFlagRegular;
+                    for (int j = 0; j < m; ++j) h_ndel.push_back(nd[j]);
+                }
                 h_meta.push_back(d);
             }
         }
+        // order the level's gate outputs by fan-in class (stable)
+        const uint32_t lv0 = ctx->drv_level_start.back();
+        std::stable_sort(h_meta.begin() + lv0, h_meta.end(), [](const DrvMeta &x, const DrvMeta &y) {
+            return fanin_class(x.m) < fanin_class(y.m);
+        });
+        uint32_t c0 = 0;
+        for (int c = 0; c < kClasses; ++c) {
+            ctx->cls_start.push_back(c0);
+            while (lv0 + c0 < h_meta.size() && fanin_class(h_meta[lv0 + c0].m) == c) ++c0;
+        }
+        ctx->cls_start.push_back((uint32_t)(h_meta.size() - lv0));
         ctx->drv_level_start.push_back((uint32_t)h_meta.size());
     }
     ctx->n_nets = nl->n_nets;
@@ -331,18 +385,24 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
         if (consumed[n] && !ctx->driven[n]) ctx->ext_inputs.push_back(n);
     }
     if (h_arcs.empty()) h_arcs.push_back(ArcDev{0, 0, 0, 0});
+    if (h_ndel.empty()) h_ndel.push_back(NetDelay{{kInf, kInf, kInf, kInf, kInf, kInf, kInf, kInf}});
     if (h_lut.empty()) h_lut.push_back(kVX);
     if (h_meta.empty()) h_meta.push_back(DrvMeta{});
     CK(ctx->meta.ensure(h_meta.size() * sizeof(DrvMeta)), "alloc meta");
     CK(ctx->arcs.ensure(h_arcs.size() * sizeof(ArcDev)), "alloc arcs");
+    CK(ctx->ndel.ensure(h_ndel.size() * sizeof(NetDelay)), "alloc net delays");
     CK(ctx->lut.ensure(h_lut.size()), "alloc lut");
     CK(cudaMemcpy(ctx->meta.p, h_meta.data(), h_meta.size() * sizeof(DrvMeta), cudaMemcpyHostToDevice), "upload meta");
     CK(cudaMemcpy(ctx->arcs.p, h_arcs.data(), h_arcs.size() * sizeof(ArcDev), cudaMemcpyHostToDevice), "upload arcs");
+    CK(cudaMemcpy(ctx->ndel.p, h_ndel.data(), h_ndel.size() * sizeof(NetDelay), cudaMemcpyHostToDevice),
+       "upload net delays");
     CK(cudaMemcpy(ctx->lut.p, h_lut.data(), h_lut.size(), cudaMemcpyHostToDevice), "upload lut");
     CK(ctx->seg_base.ensure((size_t)(ctx->max_width + 1) * 4), "alloc seg_base");
     CK(ctx->slot.ensure((size_t)(ctx->max_width + 1) * 8), "alloc slot");
-    ctx->seg_cap = std::max<uint32_t>(1u << 20, 8 * ctx->max_width + 64);
+    CK(ctx->scr.ensure((size_t)(ctx->max_width + 1) * 8), "alloc scratch offsets");
+    ctx->seg_cap = std::max<uint32_t>(1u << 21, 8 * ctx->max_width + 64);
     CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "alloc segs");
+    CK(ctx->copies.ensure((size_t)ctx->seg_cap * sizeof(CopyRec)), "alloc copies");
     ctx->loaded = true;
     return GLS_OK;
 }
@@ -350,8 +410,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
 static int upload_window(gls_ctx *ctx, Window *w)
 {
     const uint64_t n = ctx->n_nets;
-    CK(w->pool_t.ensure(w->cap * 4), "alloc pool times");
-    CK(w->pool_v.ensure(w->cap), "alloc pool values");
+    CK(w->pool.ensure(w->cap * 4), "alloc event pool");
     CK(w->net_off.ensure(n * 8), "alloc net_off");
     CK(w->net_len.ensure(n * 4), "alloc net_len");
     CK(w->init_off.ensure(n * 8), "alloc init_off");
@@ -359,12 +418,9 @@ static int upload_window(gls_ctx *ctx, Window *w)
     CK(w->saif.ensure(n * 24), "alloc saif");
     CK(w->small.ensure(256), "alloc counters");
     CK(w->stim_dev.ensure(w->stim_nets.size() * 4), "alloc stim nets");
-    if (w->stim_events) {
-        CK(cudaMemcpyAsync(w->pool_t.p, w->h_time.p, w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
-           "upload stimulus times");
-        CK(cudaMemcpyAsync(w->pool_v.p, w->h_value.p, w->stim_events, cudaMemcpyHostToDevice, ctx->stream),
-           "upload stimulus values");
-    }
+    if (w->stim_events)
+        CK(cudaMemcpyAsync(w->pool.p, w->h_words.p, w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
+           "upload stimulus");
     if (!w->h_off.ensure(n * 8) || !w->h_len.ensure(n * 4)) return fail(ctx, GLS_ENOMEM, "pinned staging");
     uint64_t *off = w->h_off.as<uint64_t>();
     uint32_t *len = w->h_len.as<uint32_t>();
@@ -405,51 +461,66 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     w->t_begin = t_begin;
     w->t_end = t_end;
     std::vector<uint8_t> seen(ctx->n_nets, 0);
-    uint64_t total = 0, maxlen = 0;
+    std::vector<uint64_t> at(st->n_nets + 1, 0);
     for (uint32_t k = 0; k < st->n_nets; ++k) {
         const uint32_t net = st->net[k];
         if (net >= ctx->n_nets) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u out of range", net); }
         if (seen[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u given twice", net); }
         if (ctx->driven[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus net %u is driven by a gate", net); }
         seen[net] = 1;
-        const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
-        if (b < a) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus ev_start not monotone"); }
-        for (uint64_t e = a; e < b; ++e) {
-            if (st->value[e] > 3) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus value %u", st->value[e]); }
-            if (st->time[e] == 0xFFFFFFFFu) { ctx->spare.push_back(w); return fail(ctx, GLS_ERANGE, "stimulus time 2^32-1"); }
-            if (e > a && st->time[e] <= st->time[e - 1]) {
-                ctx->spare.push_back(w);
-                return fail(ctx, GLS_EINVAL, "stimulus net %u: times not strictly increasing", net);
-            }
-        }
-        total += round4(b - a);
-        maxlen = std::max<uint64_t>(maxlen, b - a);
+        if (st->ev_start[k + 1] < st->ev_start[k]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "stimulus ev_start not monotone"); }
+        at[k + 1] = at[k] + round4(st->ev_start[k + 1] - st->ev_start[k]);
     }
     for (uint32_t net : ctx->ext_inputs)
         if (!seen[net]) { ctx->spare.push_back(w); return fail(ctx, GLS_EINVAL, "net %u is read by a gate but has no stimulus", net); }
-    // pack the stimulus into the pool layout (each net on a 4-event boundary)
-    w->stim_nets.assign(st->net, st->net + st->n_nets);
-    w->stim_off.resize(st->n_nets);
-    w->stim_len.resize(st->n_nets);
-    if (!w->h_time.ensure(total * 4) || !w->h_value.ensure(total)) {
+    const uint64_t total = at[st->n_nets];
+    if (!w->h_words.ensure(total * 4)) {
         ctx->spare.push_back(w);
         return fail(ctx, GLS_ENOMEM, "pinned staging of %llu events", (unsigned long long)total);
     }
-    uint64_t at = 0;
-    for (uint32_t k = 0; k < st->n_nets; ++k) {
-        const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
-        w->stim_off[k] = at;
-        w->stim_len[k] = (uint32_t)(b - a);
-        if (b > a) {
-            std::memcpy(w->h_time.as<uint32_t>() + at, st->time + a, (b - a) * 4);
-            std::memcpy(w->h_value.as<uint8_t>() + at, st->value + a, b - a);
+    // validate and pack (time << 2 | value), each net on a 4-event boundary;
+    // large stimuli are packed by several host threads
+    uint32_t *hw = w->h_words.as<uint32_t>();
+    std::atomic<int> bad(0);
+    std::atomic<uint32_t> bad_net(0);
+    auto pack = [&](uint32_t k0, uint32_t k1) {
+        for (uint32_t k = k0; k < k1; ++k) {
+            const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
+            uint32_t *o = hw + at[k];
+            uint32_t prev = 0;
+            for (uint64_t e = a; e < b; ++e) {
+                const uint32_t t = st->time[e], v = st->value[e];
+                if (v > 3 || t > kMaxTime || (e > a && t <= prev)) {
+                    bad = v > 3 ? 1 : (t > kMaxTime ? 2 : 3);
+                    bad_net = st->net[k];
+                    return;
+                }
+                prev = t;
+                *o++ = ev_word(t, v);
+            }
+            for (uint64_t e = b - a; e < round4(b - a); ++e) *o++ = kInf;
         }
-        for (uint64_t e = b - a; e < round4(b - a); ++e) {
-            w->h_time.as<uint32_t>()[at + e] = 0;
-            w->h_value.as<uint8_t>()[at + e] = kVX;
-        }
-        at += round4(b - a);
+    };
+    const unsigned hc = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (total > (1u << 20) && hc > 1 && st->n_nets > hc) {
+        std::vector<std::thread> th;
+        for (unsigned q = 0; q < hc; ++q)
+            th.emplace_back(pack, (uint32_t)((uint64_t)st->n_nets * q / hc), (uint32_t)((uint64_t)st->n_nets * (q + 1) / hc));
+        for (auto &t : th) t.join();
+    } else {
+        pack(0, st->n_nets);
     }
+    if (bad) {
+        ctx->spare.push_back(w);
+        const int b = bad;
+        return fail(ctx, b == 2 ? GLS_ERANGE : GLS_EINVAL, "stimulus net %u: %s", (unsigned)bad_net,
+                    b == 1 ? "value above 3" : b == 2 ? "time beyond the largest event time (2^30-2)"
+                                             : "times not strictly increasing");
+    }
+    w->stim_nets.assign(st->net, st->net + st->n_nets);
+    w->stim_off.assign(at.begin(), at.end() - 1);
+    w->stim_len.resize(st->n_nets);
+    for (uint32_t k = 0; k < st->n_nets; ++k) w->stim_len[k] = (uint32_t)(st->ev_start[k + 1] - st->ev_start[k]);
     w->stim_events = total;
     // initial pool capacity: stimulus plus an estimate of every gate's slot
     uint64_t cap = ctx->opts.pool_events;
@@ -463,6 +534,15 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         }
     }
     w->cap = std::max<uint64_t>(std::max<uint64_t>(cap, total + 1024), w->cap);
+    // level scratch: the widest level's fan-in events, estimated from the stimulus
+    {
+        const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
+        uint64_t want = (uint64_t)(2.0 * avg * 6.0 * ctx->max_width) + 16ull * ctx->max_width + 4096;
+        if (want > ctx->scr_cap) {
+            CK(ctx->scratch.ensure(want * 4), "alloc level scratch");
+            ctx->scr_cap = want;
+        }
+    }
     int rc = upload_window(ctx, w);
     if (rc) { free_window(w); return rc; }
     ctx->windows.push_back(w);
@@ -475,8 +555,7 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     WinDev d;
     d.net_off = w->net_off.as<uint64_t>();
     d.net_len = w->net_len.as<uint32_t>();
-    d.pool_t = w->pool_t.as<uint32_t>();
-    d.pool_v = w->pool_v.as<uint8_t>();
+    d.pool = w->pool.as<uint32_t>();
     d.saif = w->saif.as<unsigned long long>();
     unsigned long long *sm = w->small.as<unsigned long long>();
     d.top = sm;
@@ -485,7 +564,11 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     d.n_segs = reinterpret_cast<uint32_t *>(sm + 6);
     d.seg_base = ctx->seg_base.as<uint32_t>();
     d.slot = ctx->slot.as<uint64_t>();
+    d.scr = ctx->scr.as<uint64_t>();
     d.segs = ctx->segs.as<SegRec>();
+    d.copies = ctx->copies.as<CopyRec>();
+    d.scratch = ctx->scratch.as<uint32_t>();
+    d.scr_cap = ctx->scr_cap;
     d.cap = w->cap;
     d.seg_cap = ctx->seg_cap;
     d.t_begin = w->t_begin;
@@ -527,8 +610,10 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     LevelArgs a;
     a.meta = ctx->meta.as<DrvMeta>();
     a.arcs = ctx->arcs.as<ArcDev>();
+    a.ndel = ctx->ndel.as<NetDelay>();
     a.lut = ctx->lut.as<uint8_t>();
     a.seg_events = ctx->opts.seg_events;
+    a.seg_target = (uint32_t)ctx->sm_count * 2048u;
     a.def_delay = ctx->def_delay;
     for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
         a.lo = ctx->drv_level_start[L];
@@ -536,9 +621,16 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
         if (a.hi == a.lo) continue;
         launch_plan(d, a, ctx->stream);
         prof_mark(ctx);
-        launch_sim(d, a, ctx->sm_count, ctx->stream);
+        for (int c = 0; c < kClasses; ++c) {
+            const uint32_t d0 = ctx->cls_start[(kClasses + 1) * L + c], d1 = ctx->cls_start[(kClasses + 1) * L + c + 1];
+            if (d1 > d0) {
+                launch_sim(d, a, c, d0, d1, ctx->sm_count, ctx->stream);
+                ++*launches;
+            }
+        }
         prof_mark(ctx);
-        launch_combine(d, a, ctx->stream);
+        launch_link(d, a, ctx->stream);
+        launch_copy(d, a, ctx->sm_count, ctx->stream);
         prof_mark(ctx);
         *launches += 3;
     }
@@ -598,7 +690,7 @@ extern "C" int gls_run(gls_ctx *ctx)
                 segs += small[3];
                 fanin_ev += small[4];
                 pool_ev += small[0];
-                pool_bytes += w->cap * 5;
+                pool_bytes += w->cap * 4;
                 break;
             }
             if (err & (kErrRegion | kErrEmptied | kErrTime)) {
@@ -612,11 +704,15 @@ extern "C" int gls_run(gls_ctx *ctx)
             if (err & kErrSegCap) {
                 ctx->seg_cap *= 2;
                 CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "grow segs");
+                CK(ctx->copies.ensure((size_t)ctx->seg_cap * sizeof(CopyRec)), "grow copies");
+            }
+            if (err & kErrScratch) {
+                ctx->scr_cap *= 2;
+                CK(ctx->scratch.ensure(ctx->scr_cap * 4), "grow level scratch");
             }
             if (err & kErrPool) {
                 w->cap *= 2;
-                w->pool_t.release();
-                w->pool_v.release();
+                w->pool.release();
                 int rc = upload_window(ctx, w);
                 if (rc) return fail(ctx, GLS_EOVERFLOW, "event pool growth to %llu events failed: %s",
                                     (unsigned long long)w->cap, ctx->err.c_str());
@@ -702,8 +798,14 @@ extern "C" int gls_waveform(gls_ctx *ctx, uint32_t window, uint32_t net, uint32_
     }
     *n = len;
     const uint64_t k = std::min<uint64_t>(cap, len);
-    if (k && time) CK(cudaMemcpy(time, w->pool_t.as<uint32_t>() + off, k * 4, cudaMemcpyDeviceToHost), "read times");
-    if (k && value) CK(cudaMemcpy(value, w->pool_v.as<uint8_t>() + off, k, cudaMemcpyDeviceToHost), "read values");
+    if (k && (time || value)) {
+        std::vector<uint32_t> words(k);
+        CK(cudaMemcpy(words.data(), w->pool.as<uint32_t>() + off, k * 4, cudaMemcpyDeviceToHost), "read events");
+        for (uint64_t e = 0; e < k; ++e) {
+            if (time) time[e] = ev_time(words[e]);
+            if (value) value[e] = (uint8_t)ev_val(words[e]);
+        }
+    }
     return GLS_OK;
 }
 

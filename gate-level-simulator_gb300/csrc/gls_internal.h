@@ -1,14 +1,17 @@
 // Internal device-side data model of libgls (not part of the C ABI).
 //
 // HBM layout for one stimulus window:
-//   pool_t[u32] / pool_v[u8]  structure-of-arrays event pool; every net's
-//                             change list is a contiguous run starting on a
-//                             4-event (16-byte) boundary.
+//   pool[u32]        the event pool: every event is one word,
+//                    time << 2 | value (value 0, X=1, Z=2, 1=3), so a
+//                    16-byte load brings four events; every net's change
+//                    list is a contiguous run starting on a 4-event
+//                    boundary, its allocation padded to whole chunks.
 //   net_off[u64] / net_len[u32]  per net CSR into the pool.
-//   saif[u64 x 3]             T0 / T1 / TX per net.
+//   saif[u64 x 3]    T0 / T1 / TX per net.
 // Netlist (shared by all windows):
-//   DrvMeta per gate output ("driver"), ordered by level; Arc table; LUT
-//   table of 2-bit cell truth tables stored one value per byte.
+//   DrvMeta per gate output ("driver"), ordered by level and, inside a
+//   level, by fan-in class; arc and per-net delay tables; the LUT table of
+//   cell truth tables, one 2-bit value per byte.
 #pragma once
 #include <cstdint>
 
@@ -17,23 +20,34 @@ namespace gls {
 constexpr int kMaxSlots = 6;        // distinct fan-in nets per gate (MAX_IN_NUM, src/simulate.cu:25)
 constexpr int kMaxPins = 6;         // cell inputs covered by a LUT (4^6 entries)
 constexpr uint32_t kInf = 0xFFFFFFFFu;
+constexpr uint32_t kMaxTime = (1u << 30) - 2;   // largest event time a word can carry
 constexpr uint8_t kV0 = 0, kVX = 1, kVZ = 2, kV1 = 3;
+constexpr int kClasses = 4;         // fan-in classes: 1, 2, 3, 4..6 distinct input nets
+
+__host__ __device__ inline uint32_t ev_word(uint32_t t, uint32_t v) { return (t << 2) | v; }
+__host__ __device__ inline uint32_t ev_time(uint32_t w) { return w >> 2; }
+__host__ __device__ inline uint32_t ev_val(uint32_t w) { return w & 3u; }
 
 // error bits raised by kernels
 constexpr uint32_t kErrPool = 1u;       // event pool exhausted
 constexpr uint32_t kErrRegion = 2u;     // segment region overflow (internal invariant)
 constexpr uint32_t kErrEmptied = 4u;    // output list emptied (zero delay at t=0)
 constexpr uint32_t kErrSegCap = 8u;     // segment table too small
-constexpr uint32_t kErrTime = 16u;      // a time reached 2^32-1
+constexpr uint32_t kErrTime = 16u;      // an output time passed kMaxTime
+constexpr uint32_t kErrScratch = 32u;   // level scratch exhausted
+
+constexpr uint8_t kFlagIdent = 1;    // slot p feeds pin p for every pin
+constexpr uint8_t kFlagRegular = 2;  // every input net has no arc, one both-edge arc, or a posedge/negedge pair
+constexpr uint8_t kFlagFirstOut = 4; // first output of its instance (gate-event accounting)
 
 struct DrvMeta {            // one gate output; 48 bytes
     uint32_t out_net;
     uint32_t lut_off;       // byte offset of this output's truth table
-    uint32_t arc_off;       // first arc
+    uint32_t arc_off;       // first arc (irregular outputs)
     uint32_t pin_slot;      // 3 bits per pin: distinct-net slot feeding pin p
-    uint8_t n_pins, m, n_arcs, ident;   // ident: slot p feeds pin p for every p
+    uint8_t n_pins, m, n_arcs, flags;
     uint32_t net[kMaxSlots];
-    uint32_t reserved;
+    uint32_t dt_off;        // first per-net delay entry (regular outputs)
 };
 static_assert(sizeof(DrvMeta) == 48, "DrvMeta layout");
 
@@ -41,27 +55,73 @@ struct ArcDev {             // info = edge | slot << 2 ; delays already scaled a
     uint32_t info, rise, fall, pad;
 };
 
+// Per input net of a regular gate output: the delay an event on that net
+// selects, d[e * 4 + s - 1] for input edge e (0 rising, 1 falling, as
+// CheckDelay classes it) and output sense s (1 rise, 2 fall, 3 X->Z, 4 Z->X);
+// kInf where no arc applies.
+struct NetDelay {
+    uint32_t d[8];
+};
+
+// CheckDelay (src/simulate.cpp:1178-1201) as a function of (pre, cur)
+__host__ __device__ constexpr int sense_of(uint32_t pre, uint32_t cur)
+{
+    return ((pre == kV0 && cur != kV0) || (cur == kV1 && pre != kV1)) ? 1
+         : ((pre == kV1 && cur != kV1) || (cur == kV0 && pre != kV0)) ? 2
+         : (pre == kVX && cur == kVZ) ? 3
+         : (pre == kVZ && cur == kVX) ? 4 : 0;
+}
+// 3 bits per (pre * 4 + cur): the sense
+__host__ __device__ constexpr uint64_t sense_table()
+{
+    uint64_t t = 0;
+    for (uint32_t k = 0; k < 16; ++k) t |= (uint64_t)sense_of(k >> 2, k & 3u) << (3 * k);
+    return t;
+}
+// 1 bit per (last * 4 + cur): the input counts as a falling edge (sense 2)
+__host__ __device__ constexpr uint32_t neg_table()
+{
+    uint32_t t = 0;
+    for (uint32_t k = 0; k < 16; ++k) t |= (sense_of(k >> 2, k & 3u) == 2 ? 1u : 0u) << k;
+    return t;
+}
+constexpr uint64_t kSenseTab = sense_table();
+constexpr uint32_t kNegTab = neg_table();
+
 struct SegRec {             // one time segment of one gate output
-    uint32_t region;        // offset of the segment's stack inside the gate's slot
+    uint32_t region;        // offset of the segment's stack inside the gate's scratch
     uint32_t cnt;           // entries on the segment's local stack
     uint32_t min_o;         // smallest candidate output time in the segment
-    uint32_t fin;           // entries kept after combine
+    uint32_t fin;           // entries kept after linking
+};
+
+struct CopyRec {            // what k_copy does for one segment
+    uint64_t src;           // scratch index of the first kept entry
+    uint64_t dst;           // pool index it goes to
+    uint32_t n;             // entries to copy
+    uint32_t drv;           // gate output (level-relative)
+    unsigned long long cprev;  // clamped time of the final event before this segment's first
+    uint32_t pclass;        // value class of that event (0: 0, 1: 1, 2: X or Z)
+    uint32_t pad;
 };
 
 struct WinDev {
     uint64_t *net_off;
     uint32_t *net_len;
-    uint32_t *pool_t;
-    uint8_t *pool_v;
+    uint32_t *pool;
     unsigned long long *saif;   // 3 per net
     unsigned long long *top;    // pool bump pointer (events)
     unsigned long long *counters;  // [0] gate events, [1] output events, [2] segments, [3] fan-in events
     uint32_t *err;
     uint32_t *seg_base;         // per driver of the level, +1
-    uint64_t *slot;             // per driver of the level: slot start in the pool
+    uint64_t *slot;             // per driver of the level: final-list slot in the pool
+    uint64_t *scr;              // per driver of the level: segment stacks in the scratch
     SegRec *segs;
+    CopyRec *copies;            // per segment, written by k_link
     uint32_t *n_segs;
+    uint32_t *scratch;          // level scratch: segment stacks (event words)
     uint64_t cap;               // pool capacity (events)
+    uint64_t scr_cap;           // scratch capacity (events)
     uint32_t seg_cap;           // SegRec capacity
     uint64_t t_begin, t_end;
 };
@@ -69,15 +129,22 @@ struct WinDev {
 struct LevelArgs {
     const DrvMeta *meta;
     const ArcDev *arcs;
+    const NetDelay *ndel;
     const uint8_t *lut;
     uint32_t lo, hi;            // driver range of the level
-    uint32_t seg_events;        // target fan-in events per segment
+    uint32_t seg_events;        // fan-in events per segment (0: sized to fill the GPU)
+    uint32_t seg_target;        // segments per level to aim for when seg_events is 0
     uint32_t def_delay;         // delay used when no arc applies
 };
 
+// fan-in class of a gate output by its number of distinct input nets
+__host__ __device__ inline int fanin_class(int m) { return m <= 1 ? 0 : (m == 2 ? 1 : (m == 3 ? 2 : 3)); }
+
 void launch_stim_saif(const WinDev &w, const uint32_t *stim_nets, uint32_t n_stim, cudaStream_t st);
 void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st);
-void launch_sim(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st);
-void launch_combine(const WinDev &w, const LevelArgs &a, cudaStream_t st);
+void launch_sim(const WinDev &w, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
+                cudaStream_t st);
+void launch_link(const WinDev &w, const LevelArgs &a, cudaStream_t st);
+void launch_copy(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st);
 
 }  // namespace gls

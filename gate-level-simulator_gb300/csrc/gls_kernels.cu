@@ -1,16 +1,21 @@
 // Level kernels of the GB300 gate-level simulator (sm_103a).
 //
-// One level of gates is simulated by three launches:
+// One level of gates is simulated by four kinds of launches:
 //   k_plan     (1 CTA)   sizes every gate output's slot in the event pool and
-//                        splits its fan-in timeline into time segments.
-//   k_sim      (1 thread per segment) merges the segment's fan-in events,
-//                        evaluates the cell truth table, picks the SDF delay
-//                        and runs the inertial output stack of the reference
-//                        serial simulator on the segment.
-//   k_combine  (1 warp per gate output) applies the pops that later segments
-//                        make into earlier ones, settles the one undecided
-//                        duplicate at each segment bottom, compacts the list
-//                        and accumulates T0/T1/TX (fused SAIF).
+//                        its segment stacks in the level scratch, and splits
+//                        its fan-in timeline into time segments.
+//   k_sim<M>   (1 thread per segment, one instantiation per fan-in class)
+//                        merges the segment's fan-in events, evaluates the
+//                        cell truth table, picks the SDF delay and runs the
+//                        inertial output stack of the reference serial
+//                        simulator on the segment.
+//   k_link     (1 warp per gate output, a lane per segment) applies the pops
+//                        that later segments make into earlier ones, settles
+//                        the one undecided duplicate at each segment bottom
+//                        and places the segments in the gate's pool slot.
+//   k_copy     (1 warp per segment) moves the kept entries from the level
+//                        scratch into the event pool and accumulates T0/T1/TX
+//                        (fused SAIF).
 //
 // Semantics follow src/simulate.cpp:872-1506 of the reference.  Why the
 // segment split is exact: a candidate output event k (time o_k) is removed
@@ -87,19 +92,30 @@ __device__ uint32_t select_delay(const ArcDev *__restrict__ arcs, int n_arcs, ui
     return any ? mn : defd;
 }
 
-__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t *__restrict__ t, uint32_t n, uint32_t key)
+// Delay of an active step of a regular gate output: the smallest delay the
+// changed nets select for their own input edge and the output sense, or the
+// default when none applies.  Equals AddDelay (src/simulate.cpp:1012-1176)
+// whenever every input net has no arc, one both-edge arc, or one posedge and
+// one negedge arc: then a single changed net selects exactly one arc (or
+// none), and several changed nets take the minimum over their arcs.
+template <int M>
+__device__ __forceinline__ uint32_t regular_delay(const NetDelay *__restrict__ nd, uint32_t chg, int so,
+                                                  uint32_t curp, uint32_t lastp, uint32_t defd)
 {
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (t[mid] < key) lo = mid + 1; else hi = mid;
+    uint32_t d = kInf;
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        if ((chg >> j) & 1u) {
+            const uint32_t neg = (kNegTab >> (slot_val(lastp, j) * 4 + slot_val(curp, j))) & 1u;
+            d = min(d, __ldg(&nd[j].d[neg * 4 + so - 1]));
+        }
     }
-    return lo;
+    return d == kInf ? defd : d;
 }
 
 __device__ __forceinline__ uint32_t lut_index(uint32_t curp, const DrvMeta &md)
 {
-    if (md.ident) return curp & ((1u << (2 * md.n_pins)) - 1u);
+    if (md.flags & kFlagIdent) return curp & ((1u << (2 * md.n_pins)) - 1u);
     uint32_t idx = 0;
     for (int p = 0; p < md.n_pins; ++p)
         idx |= slot_val(curp, (md.pin_slot >> (3 * p)) & 7u) << (2 * p);
@@ -139,72 +155,89 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
 {
     __shared__ unsigned long long sm64[32];
     __shared__ uint32_t sm32[32];
-    __shared__ uint32_t s_seg;
+    __shared__ uint32_t s_seg[kClasses];
     __shared__ unsigned long long s_base;
     if (*w.err) return;
     const uint32_t n = a.hi - a.lo;
-    // total fan-in events of the level, to fit the segment table
-    unsigned long long e_tot = 0, g_tot = 0;
+    // fan-in events of the level per fan-in class: every class runs as its
+    // own launch, so every class is split into about seg_target segments
+    unsigned long long e_cls[kClasses] = {0, 0, 0, 0}, g_tot = 0;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         const DrvMeta &md = a.meta[a.lo + i];
-        for (int j = 0; j < md.m; ++j) e_tot += w.net_len[md.net[j]];
-        if (md.reserved) {  // first output of its instance: count fan-in per pin
+        unsigned long long E = 0;
+        for (int j = 0; j < md.m; ++j) E += w.net_len[md.net[j]];
+        const int c = fanin_class(md.m);
+#pragma unroll
+        for (int k = 0; k < kClasses; ++k) if (k == c) e_cls[k] += E;
+        if (md.flags & kFlagFirstOut) {  // first output of its instance: count fan-in per pin
             for (int p = 0; p < md.n_pins; ++p) g_tot += w.net_len[md.net[(md.pin_slot >> (3 * p)) & 7u]];
         }
     }
-    unsigned long long tot;
-    block_excl_scan<unsigned long long>(e_tot, &tot, sm64);
-    e_tot = tot;
+    unsigned long long tot, e_tot = 0;
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) {
+        block_excl_scan<unsigned long long>(e_cls[k], &tot, sm64);
+        e_cls[k] = tot;
+        e_tot += tot;
+    }
     block_excl_scan<unsigned long long>(g_tot, &tot, sm64);
     g_tot = tot;
     if (threadIdx.x == 0) {
-        uint32_t seg = max(a.seg_events, 8u);
+        unsigned long long floor_seg = 8;
         if (w.seg_cap <= n) {
             atomicOr(w.err, kErrSegCap);
         } else {
-            unsigned long long room = w.seg_cap - n;
-            unsigned long long need = (e_tot + room - 1) / room;
-            if (need > seg) seg = (uint32_t)min(need + 1, 0xFFFFFFFull);
+            const unsigned long long room = w.seg_cap - n;
+            floor_seg = max(floor_seg, (e_tot + room - 1) / room + 1);
         }
-        s_seg = seg;
+        for (int k = 0; k < kClasses; ++k) {
+            unsigned long long seg = a.seg_events;
+            if (!seg) seg = max(32ull, (e_cls[k] + a.seg_target - 1) / max(1u, a.seg_target));
+            s_seg[k] = (uint32_t)min(max(seg, floor_seg), 0x7FFFFFFFull);
+        }
         s_base = *w.top;
         atomicAdd(&w.counters[0], g_tot);
         atomicAdd(&w.counters[3], e_tot);
     }
     __syncthreads();
     if (*w.err) return;
-    const uint32_t seg = s_seg;
     const unsigned long long base = s_base;
     uint32_t run_seg = 0;
-    unsigned long long run_slot = 0;
+    unsigned long long run_slot = 0, run_scr = 0;
     for (uint32_t c = 0; c < n; c += blockDim.x) {
         const uint32_t i = c + threadIdx.x;
         uint32_t S = 0;
-        unsigned long long slot = 0;
+        unsigned long long slot = 0, scr = 0;
         if (i < n) {
             const DrvMeta &md = a.meta[a.lo + i];
             unsigned long long E = 0;
             for (int j = 0; j < md.m; ++j) E += w.net_len[md.net[j]];
+            const uint32_t seg = s_seg[fanin_class(md.m)];
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
-            slot = (E + S + 3) & ~3ull;
+            slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
+            scr = (E + S + 3) & ~3ull;      // segment stacks: events of the segment (+1 for the first)
         }
         uint32_t tS;
-        unsigned long long tSlot;
-        uint32_t xs = block_excl_scan<uint32_t>(S, &tS, sm32);
-        unsigned long long xo = block_excl_scan<unsigned long long>(slot, &tSlot, sm64);
+        unsigned long long tSlot, tScr;
+        const uint32_t xs = block_excl_scan<uint32_t>(S, &tS, sm32);
+        const unsigned long long xo = block_excl_scan<unsigned long long>(slot, &tSlot, sm64);
+        const unsigned long long xc = block_excl_scan<unsigned long long>(scr, &tScr, sm64);
         if (i < n) {
             w.seg_base[i] = run_seg + xs;
             const unsigned long long st = base + run_slot + xo;
             w.slot[i] = st;
+            w.scr[i] = run_scr + xc;
             w.net_off[a.meta[a.lo + i].out_net] = st;
         }
         run_seg += tS;
         run_slot += tSlot;
+        run_scr += tScr;
     }
     if (threadIdx.x == 0) {
         w.seg_base[n] = run_seg;
         *w.n_segs = run_seg;
         if (run_seg > w.seg_cap) atomicOr(w.err, kErrSegCap);
+        if (run_scr > w.scr_cap) atomicOr(w.err, kErrScratch);
         if (base + run_slot > w.cap) atomicOr(w.err, kErrPool);
         else *w.top = base + run_slot;
         atomicAdd(&w.counters[2], (unsigned long long)run_seg);
@@ -212,98 +245,178 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
 }
 
 // ------------------------------------------------------------------- sim
+// First index of the change list x[0..n) with time >= key, searched from a
+// guess: gallop away from the guess, then bisect.  Event lists of one gate
+// share the clock, so a position scaled from another list is usually a few
+// events off.  Compares whole words: time >= key <=> word >= key << 2.
+__device__ __forceinline__ uint32_t search_from(const uint32_t *__restrict__ x, uint32_t n, uint32_t key, uint32_t g)
+{
+    if (n == 0) return 0;
+    const uint32_t kw = key << 2;
+    if (g >= n) g = n - 1;
+    int64_t lo, hi;
+    if (x[g] < kw) {
+        int64_t a = g, b;
+        uint32_t step = 1;
+        for (;;) {
+            b = a + step;
+            if (b >= (int64_t)n) { b = n; break; }
+            if (x[b] >= kw) break;
+            a = b;
+            step <<= 1;
+        }
+        lo = a + 1; hi = b;
+    } else {
+        int64_t b = g, a;
+        uint32_t step = 1;
+        for (;;) {
+            a = b - step;
+            if (a < 0) { a = -1; break; }
+            if (x[a] < kw) break;
+            b = a;
+            step <<= 1;
+        }
+        lo = a + 1; hi = b;
+    }
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (x[mid] < kw) lo = mid + 1; else hi = mid;
+    }
+    return (uint32_t)lo;
+}
+
+__device__ __forceinline__ uint32_t sel4(const uint4 &q, uint32_t k)
+{
+    return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
+}
+
+// Buffered reader of one change list: the 16-byte chunk (4 events) holding
+// the head and the next chunk are kept in registers, so one vector load
+// serves four events.  Lists start on a 4-event boundary and their
+// allocations are padded to whole chunks.
+struct Reader {
+    uint32_t cb;        // chunk index of the list start (the list offset / 4)
+    uint32_t p, e;      // head and end index within the list
+    uint4 ct, nt;       // chunk holding the head, next chunk
+
+    __device__ __forceinline__ void start(const uint4 *__restrict__ P, uint64_t off, uint32_t p0, uint32_t e0)
+    {
+        cb = (uint32_t)(off >> 2);
+        p = p0;
+        e = e0;
+        if (p < e) {
+            const uint32_t c = cb + (p >> 2);
+            ct = __ldg(P + c);
+            if (((p >> 2) + 1) << 2 < e) nt = __ldg(P + c + 1);
+        }
+    }
+    // head event word, kInf once exhausted (kInf exceeds every event word)
+    __device__ __forceinline__ uint32_t head() const { return p < e ? sel4(ct, p & 3u) : kInf; }
+    __device__ __forceinline__ void advance(const uint4 *__restrict__ P)
+    {
+        ++p;
+        if ((p & 3u) == 0 && p < e) {
+            ct = nt;
+            if (((p >> 2) + 1) << 2 < e) nt = __ldg(P + cb + (p >> 2) + 1);
+        }
+    }
+};
+
 template <int M>
 __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t s,
-                            uint32_t S, uint32_t seg_id, uint64_t slot)
+                            uint32_t S, uint32_t seg_id, uint64_t scr)
 {
-    const uint32_t *bt[M];
-    const uint8_t *bv[M];
-    uint32_t len[M], pos[M], end[M], ht[M];
-    const int m = md.m;
+    const uint4 *P = reinterpret_cast<const uint4 *>(w.pool);
+    uint64_t off[M];
+    uint32_t len[M];
     int piv = 0;
     uint32_t plen = 0;
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-        len[j] = 0; bt[j] = w.pool_t; bv[j] = w.pool_v;
-        if (j < m) {
+        len[j] = 0; off[j] = 0;
+        if (j < md.m) {
             const uint32_t net = md.net[j];
-            const uint64_t off = w.net_off[net];
+            off[j] = w.net_off[net];
             len[j] = w.net_len[net];
-            bt[j] = w.pool_t + off;
-            bv[j] = w.pool_v + off;
             if (len[j] > plen) { plen = len[j]; piv = j; }
         }
     }
-    const uint32_t *pt = w.pool_t;
+    uint64_t poff = 0;
 #pragma unroll
-    for (int j = 0; j < M; ++j) if (j == piv) pt = bt[j];
-    const uint32_t tlo = s > 0 ? pt[(uint64_t)s * plen / S] : 0u;
-    const uint32_t thi = s + 1 < S ? pt[(uint64_t)(s + 1) * plen / S] : kInf;
+    for (int j = 0; j < M; ++j) if (j == piv) poff = off[j];
+    const uint32_t *pt = w.pool + poff;
+    const uint32_t plo = (uint32_t)((uint64_t)s * plen / S), phi = (uint32_t)((uint64_t)(s + 1) * plen / S);
+    const uint32_t tlo = s > 0 ? ev_time(pt[plo]) : 0u;
+    const uint32_t thi = s + 1 < S ? ev_time(pt[phi]) : kInf;
     uint32_t curp = 0x555u;   // every slot X
     uint32_t region = s, capn = 1;
     bool before = false;
+    Reader rd[M];
+    uint32_t hk[M];   // head word of every list with the value bits set: equal times compare equal
 #pragma unroll
     for (int j = 0; j < M; ++j) {
-        pos[j] = end[j] = 0;
-        ht[j] = kInf;
-        if (j < m) {
-            const uint32_t b = s > 0 ? lower_bound_u32(bt[j], len[j], tlo) : 0u;
-            const uint32_t e = s + 1 < S ? lower_bound_u32(bt[j], len[j], thi) : len[j];
+        uint32_t b = 0, e = 0;
+        if (j < md.m) {
+            const uint32_t gl = plen ? (uint32_t)((uint64_t)plo * len[j] / plen) : 0u;
+            const uint32_t gh = plen ? (uint32_t)((uint64_t)phi * len[j] / plen) : 0u;
+            b = s > 0 ? (j == piv ? plo : search_from(w.pool + off[j], len[j], tlo, gl)) : 0u;
+            e = s + 1 < S ? (j == piv ? phi : search_from(w.pool + off[j], len[j], thi, gh)) : len[j];
             region += b;
             capn += e - b;
-            pos[j] = b; end[j] = e;
             if (b > 0) {
-                curp = (curp & ~(3u << (2 * j))) | ((uint32_t)bv[j][b - 1] << (2 * j));
+                curp = (curp & ~(3u << (2 * j))) | (ev_val(w.pool[off[j] + b - 1]) << (2 * j));
                 before = true;
             }
-            if (b < e) ht[j] = bt[j][b];
         }
+        rd[j].start(P, off[j], b, e);
+        hk[j] = rd[j].head();
     }
     const uint8_t *lut = a.lut + md.lut_off;
-    const ArcDev *arcs = a.arcs + md.arc_off;
-    uint32_t *ot = w.pool_t + slot + region;
-    uint8_t *ov = w.pool_v + slot + region;
-    uint32_t cnt = 0, top_t = 0, top_v = kVX;
+    const NetDelay *nd = a.ndel + md.dt_off;
+    const bool regular = md.flags & kFlagRegular;
+    uint32_t *ot = w.scratch + scr + region;
+    uint32_t cnt = 0, top = 0;        // stack size and its top word
     int popped_v = -1;
-    if (s == 0) { ot[0] = 0; ov[0] = kVX; cnt = 1; }
+    if (s == 0) { top = ev_word(0, kVX); ot[0] = top; cnt = 1; }
     uint32_t fprev = before ? lut[lut_index(curp, md)] : kVX;
     uint32_t min_o = kInf;
     for (;;) {
-        uint32_t t = ht[0];
+        uint32_t mk = hk[0] | 3u;
 #pragma unroll
-        for (int j = 1; j < M; ++j) t = min(t, ht[j]);
-        if (t == kInf) break;
+        for (int j = 1; j < M; ++j) mk = min(mk, hk[j] | 3u);
+        if (mk == kInf) break;
         const uint32_t lastp = curp;
         uint32_t chg = 0;
 #pragma unroll
         for (int j = 0; j < M; ++j) {
-            if (ht[j] == t) {
+            if ((hk[j] | 3u) == mk) {
                 chg |= 1u << j;
-                const uint32_t v = bv[j][pos[j]];
-                curp = (curp & ~(3u << (2 * j))) | (v << (2 * j));
-                ++pos[j];
-                ht[j] = pos[j] < end[j] ? bt[j][pos[j]] : kInf;
+                curp = (curp & ~(3u << (2 * j))) | (ev_val(hk[j]) << (2 * j));
+                rd[j].advance(P);
+                hk[j] = rd[j].head();
             }
         }
         const uint32_t F = lut[lut_index(curp, md)];
         if (F == fprev) continue;
-        const int so = check_delay(fprev, F);
+        const int so = (int)((kSenseTab >> (3 * (fprev * 4 + F))) & 7u);
         fprev = F;
-        const uint32_t d = select_delay(arcs, md.n_arcs, chg, so, curp, lastp, a.def_delay);
+        const uint32_t t = ev_time(mk);
+        const uint32_t d = regular ? regular_delay<M>(nd, chg, so, curp, lastp, a.def_delay)
+                                   : select_delay(a.arcs + md.arc_off, md.n_arcs, chg, so, curp, lastp, a.def_delay);
         const uint32_t o = t + d;
-        if (o < t || o == kInf) { atomicOr(w.err, kErrTime); break; }
+        if (o > kMaxTime || o < t) { atomicOr(w.err, kErrTime); break; }
         min_o = min(min_o, o);
         // inertial update, src/simulate.cpp:991-1009
-        while (cnt > 0 && top_t >= o) {
-            if (s == 0 && cnt == 1) { popped_v = (int)top_v; cnt = 0; break; }
+        while (cnt > 0 && ev_time(top) >= o) {
+            if (s == 0 && cnt == 1) { popped_v = (int)ev_val(top); cnt = 0; break; }
             --cnt;
-            if (cnt > 0) { top_t = ot[cnt - 1]; top_v = ov[cnt - 1]; }
+            if (cnt > 0) top = ot[cnt - 1];
         }
-        const int prevv = cnt > 0 ? (int)top_v : (s == 0 ? popped_v : -1);
+        const int prevv = cnt > 0 ? (int)ev_val(top) : (s == 0 ? popped_v : -1);
         if (prevv != (int)F) {
             if (cnt >= capn) { atomicOr(w.err, kErrRegion); break; }
-            ot[cnt] = o; ov[cnt] = (uint8_t)F;
-            ++cnt; top_t = o; top_v = F;
+            top = ev_word(o, F);
+            ot[cnt++] = top;
         } else if (cnt == 0) {
             atomicOr(w.err, kErrEmptied);
             break;
@@ -314,26 +427,36 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     w.segs[seg_id] = r;
 }
 
-__global__ void __launch_bounds__(128) k_sim(WinDev w, LevelArgs a)
+// Gates of a level are sorted by fan-in class; one instantiation per class
+// keeps the register budget of the common narrow gates small.  Each block
+// owns a contiguous share of the class's segments and its threads take the
+// next one from a shared counter as they finish, so long and short segments
+// balance inside the block.
+template <int M>
+__global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4)) k_sim(WinDev w, LevelArgs a, uint32_t d0, uint32_t d1)
 {
+    __shared__ uint32_t s_next;
     if (*w.err) return;
-    const uint32_t n = a.hi - a.lo;
-    const uint32_t nseg = *w.n_segs;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < nseg; g += gridDim.x * blockDim.x) {
-        // driver owning segment g: last i with seg_base[i] <= g
-        uint32_t lo = 0, hi = n;
+    const uint32_t g0 = w.seg_base[d0], g1 = w.seg_base[d1];
+    const uint32_t total = g1 - g0;
+    const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
+    const uint32_t b0 = g0 + min(total, blockIdx.x * per), b1 = g0 + min(total, (blockIdx.x + 1) * per);
+    if (threadIdx.x == 0) s_next = b0;
+    __syncthreads();
+    for (;;) {
+        const uint32_t g = atomicAdd(&s_next, 1u);
+        if (g >= b1) break;
+        // driver owning segment g: last i in [d0, d1) with seg_base[i] <= g
+        uint32_t lo = d0, hi = d1;
         while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
+            const uint32_t mid = (lo + hi) >> 1;
             if (w.seg_base[mid] <= g) lo = mid; else hi = mid;
         }
         const uint32_t i = lo;
         const uint32_t sb = w.seg_base[i];
         const uint32_t S = w.seg_base[i + 1] - sb;
         const DrvMeta md = a.meta[a.lo + i];
-        const uint64_t slot = w.slot[i];
-        if (md.m <= 2) sim_segment<2>(w, a, md, g - sb, S, g, slot);
-        else if (md.m == 3) sim_segment<3>(w, a, md, g - sb, S, g, slot);
-        else sim_segment<kMaxSlots>(w, a, md, g - sb, S, g, slot);
+        sim_segment<M>(w, a, md, g - sb, S, g, w.scr[i]);
     }
 }
 
@@ -345,46 +468,30 @@ __device__ __forceinline__ unsigned long long clampt(uint32_t t, unsigned long l
 }
 __device__ __forceinline__ int vclass(uint32_t v) { return v == kV0 ? 0 : (v == kV1 ? 1 : 2); }
 
-// Copy `n` events from pool[src..] to pool[dst..] (dst <= src) and add their
-// SAIF contributions: event i holds the net from its time until the next
-// event, clipped to [t_begin, t_end) (src/simulate.cpp:102-163).
-__device__ void copy_and_integrate(const WinDev &w, uint64_t src, uint64_t dst, uint32_t n,
-                                   unsigned long long &cprev, int &pclass, unsigned long long acc[3])
+__device__ __forceinline__ void saif_add(unsigned long long acc[3], int cls, unsigned long long d)
 {
-    const int lane = threadIdx.x & 31;
-    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
-        const uint32_t i = i0 + lane;
-        const bool v = i < n;
-        uint32_t t = 0, val = 0;
-        if (v) { t = w.pool_t[src + i]; val = w.pool_v[src + i]; }
-        __syncwarp();
-        if (v && src != dst) { w.pool_t[dst + i] = t; w.pool_v[dst + i] = (uint8_t)val; }
-        const unsigned long long c = clampt(t, w.t_begin, w.t_end);
-        unsigned long long cp = __shfl_up_sync(0xffffffffu, c, 1);
-        int pc = __shfl_up_sync(0xffffffffu, vclass(val), 1);
-        if (lane == 0) { cp = cprev; pc = pclass; }
-        if (v) {
-            const unsigned long long dlt = c - cp;
-            if (pc == 0) acc[0] += dlt; else if (pc == 1) acc[1] += dlt; else acc[2] += dlt;
-        }
-        const int last = (int)min(31u, n - 1 - i0);
-        cprev = __shfl_sync(0xffffffffu, c, last);
-        pclass = __shfl_sync(0xffffffffu, vclass(val), last);
-    }
+    if (cls == 0) acc[0] += d; else if (cls == 1) acc[1] += d; else acc[2] += d;
 }
 
-__global__ void __launch_bounds__(256) k_combine(WinDev w, LevelArgs a)
+// k_link: one warp per gate output, a lane per segment.  Pass A cuts each
+// segment's stack at the smallest candidate time of the later segments;
+// pass B drops a segment's first entry when it repeats the last kept value
+// before it, places the segments back to back in the gate's pool slot and
+// hands each segment's copy to k_copy with the final event that precedes it.
+__global__ void __launch_bounds__(256) k_link(WinDev w, LevelArgs a)
 {
     if (*w.err) return;
     const uint32_t n = a.hi - a.lo;
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
+    const unsigned FULL = 0xffffffffu;
     const uint32_t sb = w.seg_base[i], se = w.seg_base[i + 1];
     const uint64_t slot = w.slot[i];
+    const uint64_t scr = w.scr[i];
+    const uint32_t *sx = w.scratch + scr;
     const uint32_t out_net = a.meta[a.lo + i].out_net;
-    // pass A (right to left): cut each segment's stack at the smallest
-    // candidate time of all later segments.
+    // pass A (right to left)
     uint32_t carry_min = kInf;
     for (int64_t base = se; base > (int64_t)sb; base -= 32) {
         const int64_t s = base - 32 + lane;
@@ -394,78 +501,163 @@ __global__ void __launch_bounds__(256) k_combine(WinDev w, LevelArgs a)
         uint32_t x = r.min_o;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_down_sync(0xffffffffu, x, o);
+            const uint32_t y = __shfl_down_sync(FULL, x, o);
             if (lane + o < 32) x = min(x, y);
         }
-        uint32_t ex = __shfl_down_sync(0xffffffffu, x, 1);
+        uint32_t ex = __shfl_down_sync(FULL, x, 1);
         if (lane == 31) ex = kInf;
         const uint32_t M = min(ex, carry_min);
         if (valid) {
-            const uint32_t keep = lower_bound_u32(w.pool_t + slot + r.region, r.cnt, M);
+            uint32_t keep = r.cnt;   // stack times increase: cut from the top
+            while (keep > 0 && ev_time(sx[r.region + keep - 1]) >= M) --keep;
             w.segs[s].fin = keep;
         }
-        carry_min = min(carry_min, __shfl_sync(0xffffffffu, x, 0));
+        carry_min = min(carry_min, __shfl_sync(FULL, x, 0));
     }
     __syncwarp();
-    // pass B (left to right): settle the bottom entry of every segment after
-    // the first, place the segments back to back, integrate SAIF.
-    uint32_t carry_pos = 0;
-    uint32_t carry_v = kVX;
-    unsigned long long cprev = w.t_begin;
-    int pclass = 2;
-    unsigned long long acc[3] = {0, 0, 0};
+    // pass B (left to right)
+    uint32_t carry_pos = 0, carry_v = kVX;
+    unsigned long long cprev = w.t_begin;    // clamped time of the previous final event
+    int pclass = 2;                          // its value class
     for (uint32_t base = sb; base < se; base += 32) {
         const uint32_t s = base + lane;
         const bool valid = s < se;
-        uint32_t keep = 0, region = 0, firstv = 0, lastv = 0;
+        uint32_t keep = 0, region = 0, firstv = 0, lastv = 0, lastt = 0;
         if (valid) {
             const SegRec r = w.segs[s];
             keep = r.fin;
             region = r.region;
             if (keep) {
-                firstv = w.pool_v[slot + region];
-                lastv = w.pool_v[slot + region + keep - 1];
+                firstv = ev_val(sx[region]);
+                const uint32_t lw = sx[region + keep - 1];
+                lastv = ev_val(lw);
+                lastt = ev_time(lw);
             }
         }
-        const unsigned bal = __ballot_sync(0xffffffffu, keep > 0);
+        const unsigned bal = __ballot_sync(FULL, keep > 0);
         const unsigned prior = bal & ((1u << lane) - 1u);
-        const int srcl = prior ? 31 - __clz(prior) : 0;
-        const uint32_t vsh = __shfl_sync(0xffffffffu, lastv, srcl);
+        const uint32_t vsh = __shfl_sync(FULL, lastv, prior ? 31 - __clz(prior) : 0);
         const uint32_t vprev = prior ? vsh : carry_v;
         const uint32_t drop = (s > sb && keep > 0 && firstv == vprev) ? 1u : 0u;
         const uint32_t fin = keep - drop;
         uint32_t inc = fin;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            const uint32_t y = __shfl_up_sync(FULL, inc, o);
             if (lane >= o) inc += y;
         }
         const uint32_t pos = carry_pos + inc - fin;
-        if (bal) carry_v = __shfl_sync(0xffffffffu, lastv, 31 - __clz(bal));
-        carry_pos += __shfl_sync(0xffffffffu, inc, 31);
-        const uint32_t cnt_here = min(32u, se - base);
-        for (uint32_t k = 0; k < cnt_here; ++k) {
-            const uint32_t kf = __shfl_sync(0xffffffffu, fin, k);
-            const uint32_t kr = __shfl_sync(0xffffffffu, region + drop, k);
-            const uint32_t kp = __shfl_sync(0xffffffffu, pos, k);
-            if (kf) copy_and_integrate(w, slot + kr, slot + kp, kf, cprev, pclass, acc);
+        const unsigned fb = __ballot_sync(FULL, fin > 0);
+        const unsigned fprior = fb & ((1u << lane) - 1u);
+        const int fsrc = fprior ? 31 - __clz(fprior) : 0;
+        const unsigned long long clast = clampt(lastt, w.t_begin, w.t_end);
+        const unsigned long long csh = __shfl_sync(FULL, clast, fsrc);
+        const int ksh = __shfl_sync(FULL, vclass(lastv), fsrc);
+        if (valid) {
+            CopyRec c;
+            c.src = scr + region + drop;
+            c.dst = slot + pos;
+            c.n = fin;
+            c.drv = i;
+            c.cprev = fprior ? csh : cprev;
+            c.pclass = (uint32_t)(fprior ? ksh : pclass);
+            c.pad = 0;
+            w.copies[s] = c;
         }
+        if (bal) carry_v = __shfl_sync(FULL, lastv, 31 - __clz(bal));
+        if (fb) {
+            const int top = 31 - __clz(fb);
+            cprev = __shfl_sync(FULL, clast, top);
+            pclass = __shfl_sync(FULL, vclass(lastv), top);
+        }
+        carry_pos += __shfl_sync(FULL, inc, 31);
     }
-    // the last event holds until t_end
     if (lane == 0) {
-        const unsigned long long dlt = w.t_end - cprev;
-        if (pclass == 0) acc[0] += dlt; else if (pclass == 1) acc[1] += dlt; else acc[2] += dlt;
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
-    if (lane == 0) {
+        // the last event holds until t_end; k_copy adds the rest
+        unsigned long long acc[3] = {0, 0, 0};
+        saif_add(acc, pclass, w.t_end - cprev);
         w.net_len[out_net] = carry_pos;
         w.saif[3ull * out_net + 0] = acc[0];
         w.saif[3ull * out_net + 1] = acc[1];
         w.saif[3ull * out_net + 2] = acc[2];
         atomicAdd(&w.counters[1], (unsigned long long)carry_pos);
+    }
+}
+
+// SAIF contributions of W consecutive events of a list held one per lane of
+// a W-lane group: an event holds the net from its time to the next event's,
+// clipped to [t_begin, t_end) (src/simulate.cpp:102-163).  (cprev, pclass)
+// describe the event before the group's first and are advanced past its last.
+template <int W>
+__device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, bool v, uint32_t n_here, bool any,
+                                                unsigned long long &cprev, int &pclass, unsigned long long acc[3])
+{
+    const unsigned FULL = 0xffffffffu;
+    const int sub = threadIdx.x & (W - 1);
+    const unsigned long long ct = clampt(ev_time(word), w.t_begin, w.t_end);
+    const int cl = vclass(ev_val(word));
+    unsigned long long cp = __shfl_up_sync(FULL, ct, 1, W);
+    int pc = __shfl_up_sync(FULL, cl, 1, W);
+    if (sub == 0) { cp = cprev; pc = pclass; }
+    if (v) saif_add(acc, pc, ct - cp);
+    const int last = (int)min((uint32_t)(W - 1), n_here - 1);
+    const unsigned long long cn = __shfl_sync(FULL, ct, last, W);
+    const int pn = __shfl_sync(FULL, cl, last, W);
+    if (any) { cprev = cn; pclass = pn; }
+}
+
+// k_copy: one 16-lane group per segment: copy the kept entries from the
+// level scratch into the pool and add their SAIF contributions to the gate
+// output's counters.  The next segment's record is loaded while the current
+// one is copied.
+__global__ void __launch_bounds__(256) k_copy(WinDev w, LevelArgs a)
+{
+    constexpr int W = 16;
+    const unsigned FULL = 0xffffffffu;
+    if (*w.err) return;
+    const int sub = threadIdx.x & (W - 1);
+    const uint32_t nseg = *w.n_segs;
+    const uint32_t gpb = blockDim.x / W;
+    const uint32_t stride = gridDim.x * gpb;
+    uint32_t s = blockIdx.x * gpb + threadIdx.x / W;
+    // every group of a warp runs the same number of rounds (shuffles need the full warp)
+    const uint32_t warp_first = blockIdx.x * gpb + (threadIdx.x & ~31u) / W;
+    const uint32_t rounds = warp_first < nseg ? (nseg - warp_first + stride - 1) / stride : 0;
+    CopyRec c = {0, 0, 0, 0, 0, 0, 0};
+    if (s < nseg) c = w.copies[s];
+    for (uint32_t r = 0; r < rounds; ++r, s += stride) {
+        CopyRec nx = {0, 0, 0, 0, 0, 0, 0};
+        if (s + stride < nseg) nx = w.copies[s + stride];
+        const bool live = s < nseg && c.n > 0;
+        unsigned long long acc[3] = {0, 0, 0};
+        unsigned long long cprev = c.cprev;
+        int pclass = (int)c.pclass;
+        const uint32_t n = live ? c.n : 0;
+        // groups of one warp may have different lengths: loop to the warp's longest
+        uint32_t nmax = n;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
+        for (uint32_t i0 = 0; i0 < nmax; i0 += W) {
+            const uint32_t i = i0 + sub;
+            const bool v = i < n;
+            uint32_t word = 0;
+            if (v) {
+                word = w.scratch[c.src + i];
+                w.pool[c.dst + i] = word;
+            }
+            integrate_group<W>(w, word, v, i0 < n ? n - i0 : 1u, i0 < n, cprev, pclass, acc);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int o = W / 2; o > 0; o >>= 1) acc[k] += __shfl_down_sync(FULL, acc[k], o, W);
+        if (sub == 0 && live) {
+            const uint32_t out_net = a.meta[a.lo + c.drv].out_net;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (acc[k]) atomicAdd(&w.saif[3ull * out_net + k], acc[k]);
+        }
+        c = nx;
     }
 }
 
@@ -481,11 +673,12 @@ __global__ void __launch_bounds__(256) k_stim_saif(WinDev w, const uint32_t *__r
     unsigned long long cprev = w.t_begin;
     int pclass = 2;
     unsigned long long acc[3] = {0, 0, 0};
-    copy_and_integrate(w, off, off, len, cprev, pclass, acc);
-    if (lane == 0) {
-        const unsigned long long dlt = w.t_end - cprev;
-        if (pclass == 0) acc[0] += dlt; else if (pclass == 1) acc[1] += dlt; else acc[2] += dlt;
+    for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+        const bool v = i0 + lane < len;
+        const uint32_t word = v ? w.pool[off + i0 + lane] : 0u;
+        integrate_group<32>(w, word, v, len - i0, true, cprev, pclass, acc);
     }
+    if (lane == 0) saif_add(acc, pclass, w.t_end - cprev);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -509,16 +702,27 @@ void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st)
     k_plan<<<1, 1024, 0, st>>>(w, a);
 }
 
-void launch_sim(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st)
+void launch_sim(const WinDev &w, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count, cudaStream_t st)
 {
-    k_sim<<<sm_count * 16, 128, 0, st>>>(w, a);
+    const int grid = sm_count * (cls <= 1 ? 8 : (cls == 2 ? 6 : 4));
+    switch (cls) {
+    case 0: k_sim<1><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
+    case 1: k_sim<2><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
+    case 2: k_sim<3><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
+    default: k_sim<kMaxSlots><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
+    }
 }
 
-void launch_combine(const WinDev &w, const LevelArgs &a, cudaStream_t st)
+void launch_link(const WinDev &w, const LevelArgs &a, cudaStream_t st)
 {
     const uint32_t n = a.hi - a.lo;
     const uint32_t blocks = (uint32_t)(((uint64_t)n * 32 + 255) / 256);
-    k_combine<<<blocks, 256, 0, st>>>(w, a);
+    k_link<<<blocks, 256, 0, st>>>(w, a);
+}
+
+void launch_copy(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st)
+{
+    k_copy<<<sm_count * 8, 256, 0, st>>>(w, a);
 }
 
 }  // namespace gls
