@@ -17,97 +17,9 @@
 #include <vector>
 #include "gls.h"
 #include "gls_internal.h"
+#include "gls_ctx.h"
 
 using namespace gls;
-
-namespace {
-
-struct DevBuf {
-    void *p = nullptr;
-    size_t bytes = 0;
-    cudaError_t ensure(size_t n)
-    {
-        if (n <= bytes && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, n ? n : 16);
-        if (e == cudaSuccess) bytes = n ? n : 16;
-        return e;
-    }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T *as() const { return static_cast<T *>(p); }
-};
-
-struct PinBuf {   // page-locked host staging, reused across windows
-    void *p = nullptr;
-    size_t bytes = 0;
-    bool ensure(size_t n)
-    {
-        if (n <= bytes && p) return true;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        if (cudaHostAlloc(&p, n ? n : 16, cudaHostAllocDefault) != cudaSuccess) return false;
-        bytes = n ? n : 16;
-        return true;
-    }
-    void release()
-    {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T *as() const { return static_cast<T *>(p); }
-};
-
-struct Window {
-    std::vector<uint32_t> stim_nets;
-    std::vector<uint64_t> stim_off;     // aligned pool offset per stimulus net
-    std::vector<uint32_t> stim_len;
-    uint64_t stim_events = 0;           // aligned extent of the stimulus in the pool
-    PinBuf h_words;                     // packed stimulus events (kept to re-upload on pool growth)
-    PinBuf h_off, h_len;                // initial net table
-    uint64_t t_begin = 0, t_end = 0;
-    uint64_t cap = 0;
-    DevBuf pool, net_off, net_len, init_off, init_len, saif, small, stim_dev;
-    bool done = false;
-};
-
-}  // namespace
-
-struct gls_ctx {
-    gls_opts opts{};
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int sm_count = 0;
-    std::string err;
-    bool loaded = false;
-    uint32_t n_nets = 0;
-    uint32_t n_drv = 0;
-    std::vector<uint32_t> drv_level_start;   // per level, into drivers
-    std::vector<uint32_t> cls_start;         // per level kClasses+1 entries: fan-in class ranges, level-relative
-    uint32_t max_width = 0;
-    uint64_t pins_total = 0;
-    std::vector<uint8_t> driven;             // net driven by a gate output
-    std::vector<uint32_t> ext_inputs;        // nets read by gates and driven by no gate
-    DevBuf meta, arcs, ndel, lut;
-    DevBuf seg_base, slot, scr, segs, copies, scratch;
-    uint32_t seg_cap = 0;
-    uint64_t scr_cap = 0;
-    uint32_t def_delay = 1;
-    std::vector<Window *> windows;
-    std::vector<Window *> spare;     // cleared windows whose buffers are reused
-    gls_stats stats{};
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::vector<cudaEvent_t> prof;   // per-launch events when opts.profile
-    size_t prof_used = 0;
-};
 
 namespace {
 
@@ -121,6 +33,33 @@ int fail(gls_ctx *c, int code, const char *fmt, ...)
     if (c) c->err = buf;
     return code;
 }
+
+}  // namespace
+
+int ctx_fail(gls_ctx *c, int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
+{
+    a->meta = ctx->meta.as<DrvMeta>();
+    a->arcs = ctx->arcs.as<ArcDev>();
+    a->ndel = ctx->ndel.as<NetDelay>();
+    a->lut = ctx->lut.as<uint8_t>();
+    a->lo = a->hi = 0;
+    a->seg_events = ctx->opts.seg_events;
+    a->seg_target = (uint32_t)ctx->sm_count * 2048u;
+    a->def_delay = ctx->def_delay;
+}
+
+namespace {
 
 int cuda_fail(gls_ctx *c, cudaError_t e, const char *what)
 {

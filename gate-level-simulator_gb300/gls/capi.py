@@ -23,7 +23,7 @@ ALLOC_BOUND, ALLOC_EXACT = 0, 1
 # every symbol include/gls.h declares
 EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "gls_add_window",
             "gls_clear_windows", "gls_run", "gls_saif_counts", "gls_waveform_lengths", "gls_waveform",
-            "gls_stats_get", "gls_cell_lut", "gls_abi_version"]
+            "gls_stats_get", "gls_cell_lut", "gls_abi_version", "gls_run_level_static"]
 
 
 class GlsError(RuntimeError):
@@ -90,6 +90,8 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_stats_get.argtypes = [C.c_void_p, C.POINTER(Stats)]
     lib.gls_cell_lut.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_uint32]
     lib.gls_abi_version.restype = C.c_int
+    lib.gls_run_level_static.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]
     if path is None:
         _lib = lib
     return lib
@@ -209,6 +211,13 @@ class Simulator:
         v = np.zeros(n.value, np.uint8)
         self._check(self.lib.gls_waveform(self.h, window, net, _ptr(t), _ptr(v), n.value, C.byref(n)), "waveform")
         return t, v
+
+    def run_level_static(self, level: int, first: int, count: int, d_pool: int, pool_cap: int, d_top: int,
+                         d_net_off: int, d_net_len: int, d_saif: int, t_begin: int, t_end: int):
+        """One level's gate outputs on caller-owned device buffers (device
+        pointers as integers), with no device allocation by the library."""
+        self._check(self.lib.gls_run_level_static(self.h, level, first, count, d_pool, pool_cap, d_top, d_net_off,
+                                                  d_net_len, d_saif, t_begin, t_end), "run_level_static")
 
     def stats(self) -> dict:
         s = Stats()

@@ -191,6 +191,42 @@ int gls_cell_lut(const gls_cell *cell, const gls_prim *prims, int out,
 
 int gls_abi_version(void);
 
+/* Simulate gate outputs [first, first + count) of one level (in the
+ * library's order inside the level; count up to the level's number of gate
+ * outputs) without allocating any device memory.  This entry point has no
+ * counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc while they simulate, e.g.
+ * an application that owns all device memory through its own arena, or a
+ * latency-bound loop that cannot pay the device synchronization that
+ * cudaMalloc / cudaFree can cause.  Such a caller passes its own device
+ * buffers for the inputs and outputs:
+ *   d_pool     the event pool, one 32-bit word per event, time << 2 | value
+ *              (times up to 2^30 - 2); every change list starts on a 4-word
+ *              boundary and its allocation is padded to a multiple of 4 words
+ *   pool_cap   capacity of d_pool in words
+ *   d_top      one 64-bit word: first free pool word; output lists are
+ *              appended there (4-word aligned) and it is advanced
+ *   d_net_off / d_net_len   per net: pool offset and length; read for the
+ *              gate inputs, written for the gate outputs
+ *   d_saif     3 x 64-bit per net (T0, T1, TX over [t_begin, t_end)),
+ *              written for the gate outputs
+ * The segment stacks and segment tables live in one static device array of
+ * 20,775,936 bytes (about 20 MiB) that every GPU loading the library holds
+ * until exit.  One
+ * call handles at most 16384 gate outputs, 65536 time segments and
+ * 4194304 segment-stack words; larger requests fail with GLS_ERANGE and a
+ * message (pass fewer outputs per call).  The call waits for its kernels
+ * (on the context's stream) to finish.  The first call on a device looks up
+ * the static array's device address; make that first call before any
+ * stream capture.  All calls on a device share the array: calls that
+ * overlap on the GPU (other threads, other contexts of the same device)
+ * race and must be serialized by the caller. */
+int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first, uint32_t count,
+                         uint32_t *d_pool, uint64_t pool_cap, unsigned long long *d_top,
+                         uint64_t *d_net_off, uint32_t *d_net_len,
+                         unsigned long long *d_saif, uint64_t t_begin, uint64_t t_end);
+
 #ifdef __cplusplus
 }
 #endif
