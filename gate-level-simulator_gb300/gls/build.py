@@ -65,6 +65,9 @@ def build_lib(force: bool = False) -> Path:
 
 def build_all(force: bool = False) -> None:
     build_lib(force)
+    from . import hostbuild   # the command-line tools
+
+    hostbuild.build(force)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,50 @@
+// gls_process <vlib> <gv> <sdf> <inter.dat>
+//
+// The `process` step of the reference (src/process.cpp:178-610): read the
+// Verilog cell library, the flat gate-level netlist and the SDF file,
+// levelize the instance graph and write the levelized design to inter.dat
+// (native binary format; see host/design.cpp).
+#include <cstdio>
+#include <string>
+#include "design.h"
+
+int main(int argc, char **argv)
+{
+    if (argc != 5) {
+        printf("[USAGE] ./gls_process vlib_path gv_path sdf_path intermediate_file\n");
+        return 255;
+    }
+    using namespace glsh;
+    std::string err;
+    Library lib;
+    Design d;
+    const std::string vlib = read_file(argv[1], &err);
+    if (vlib.empty() || !parse_vlib(vlib, lib, &err)) {
+        printf("ERROR: %s\n", err.empty() ? "empty cell library" : err.c_str());
+        return 255;
+    }
+    printf("INFO: vlib file's parsing done! (%zu modules, %zu skipped)\n", lib.cells.size(), lib.ignored.size());
+    const std::string gv = read_file(argv[2], &err);
+    if (gv.empty() || !parse_gv(gv, lib, d, &err)) {
+        printf("ERROR: %s\n", err.empty() ? "empty netlist" : err.c_str());
+        return 255;
+    }
+    printf("INFO: gate level file's parsing done! (%zu instances, %zu nets)\n", d.insts.size(), d.net_names.size());
+    const std::string sdf = read_file(argv[3], &err);
+    if (!sdf.empty() && !parse_sdf(sdf, d, lib, &err)) {
+        printf("ERROR: %s\n", err.c_str());
+        return 255;
+    }
+    printf("INFO: SDF file's parsing done!\n");
+    if (!levelize(d, &err)) {
+        printf("ERROR: %s\n", err.c_str());
+        return 255;
+    }
+    printf("levels size: %zu\n", d.level_start.size() - 1);
+    if (!write_inter(argv[4], d, &err)) {
+        printf("ERROR: %s\n", err.c_str());
+        return 255;
+    }
+    printf("store database into %s\n", argv[4]);
+    return 0;
+}

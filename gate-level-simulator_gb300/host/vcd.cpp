@@ -1,0 +1,191 @@
+// VCD reader of the gls command-line tools.
+//
+// Reads what the reference's VCDParser reads (src/VCDParser.cpp:283-717):
+// $timescale, $var declarations (scalars and buses with [msb:lsb] ranges,
+// bit-blasted into name[i]), #time lines, scalar changes and b<bits>
+// vector changes.  Real values are ignored.  Short vector values are
+// extended on the left as VCD specifies (the reference indexes the string
+// as if it were full width).
+#include "vcd.h"
+
+#include <cctype>
+#include <cstdlib>
+#include <cstring>
+
+namespace glsh {
+
+namespace {
+
+uint8_t code(char c)
+{
+    switch (c) {
+    case '0': return 0;
+    case '1': return 3;
+    case 'x': case 'X': return 1;
+    case 'z': case 'Z': return 2;
+    default: return 255;
+    }
+}
+
+struct Var {
+    std::vector<size_t> bits;   // signal index per value-string position (msb first)
+    bool bus;
+};
+
+}  // namespace
+
+bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
+{
+    size_t i = 0;
+    auto tok = [&](std::string &t) -> bool {
+        while (i < s.size() && isspace((unsigned char)s[i])) ++i;
+        if (i >= s.size()) return false;
+        size_t j = i;
+        while (j < s.size() && !isspace((unsigned char)s[j])) ++j;
+        t.assign(s, i, j - i);
+        i = j;
+        return true;
+    };
+    auto skip_to_end = [&]() {
+        std::string t;
+        while (tok(t) && t != "$end") {}
+    };
+    std::unordered_map<std::string, std::vector<Var>> vars;   // id -> declarations
+    auto signal = [&](const std::string &name) -> size_t {
+        auto it = v.index.find(name);
+        if (it != v.index.end()) return it->second;
+        const size_t k = v.names.size();
+        v.index.emplace(name, k);
+        v.names.push_back(name);
+        v.times.emplace_back();
+        v.values.emplace_back();
+        return k;
+    };
+    std::string t;
+    // ---------------------------------------------------------- header
+    for (;;) {
+        if (!tok(t)) {
+            if (err) *err = "VCD: no $enddefinitions";
+            return false;
+        }
+        if (t == "$enddefinitions") { skip_to_end(); break; }
+        if (t == "$timescale") {
+            std::string a, all;
+            while (tok(a) && a != "$end") all += a;
+            size_t k = 0;
+            while (k < all.size() && isdigit((unsigned char)all[k])) ++k;
+            v.time_res = k ? (unsigned)atoi(all.substr(0, k).c_str()) : 1u;
+            v.time_unit = all.substr(k);
+            continue;
+        }
+        if (t == "$var") {
+            std::vector<std::string> f;
+            std::string a;
+            while (tok(a) && a != "$end") f.push_back(a);
+            if (f.size() < 4) {
+                if (err) *err = "VCD: short $var";
+                return false;
+            }
+            const int size = atoi(f[1].c_str());
+            const std::string id = f[2];
+            std::string ref = f[3];
+            std::string range = f.size() > 4 ? f[4] : std::string();
+            const size_t br = ref.find('[');
+            if (range.empty() && br != std::string::npos) {
+                range = ref.substr(br);
+                ref = ref.substr(0, br);
+            }
+            Var var;
+            var.bus = false;
+            if (size <= 1) {
+                std::string name = ref;
+                if (!range.empty()) {
+                    const std::string inner = range.substr(1, range.find(']') - 1);
+                    const size_t c = inner.find(':');
+                    name = ref + "[" + (c == std::string::npos ? inner : inner.substr(0, c)) + "]";
+                }
+                var.bits.push_back(signal(name));
+            } else {
+                int l = size - 1, r = 0;
+                if (!range.empty()) {
+                    const std::string inner = range.substr(1, range.find(']') - 1);
+                    const size_t c = inner.find(':');
+                    if (c != std::string::npos) {
+                        l = atoi(inner.substr(0, c).c_str());
+                        r = atoi(inner.substr(c + 1).c_str());
+                    }
+                }
+                var.bus = true;
+                for (int b = l;; b += (r > l ? 1 : -1)) {
+                    var.bits.push_back(signal(ref + "[" + std::to_string(b) + "]"));
+                    if (b == r) break;
+                }
+            }
+            vars[id].push_back(var);
+            continue;
+        }
+        if (t[0] == '$') skip_to_end();
+    }
+    // ------------------------------------------------------------ body
+    std::vector<uint8_t> last(v.names.size(), 2);   // bus bits: the last value kept, starting from Z
+    uint64_t now = 0;
+    auto put = [&](size_t k, uint8_t val, bool dedup) {
+        auto &tt = v.times[k];
+        auto &vv = v.values[k];
+        if (dedup) {
+            if (val == last[k]) return;
+            last[k] = val;
+        }
+        if (!tt.empty() && tt.back() == now) {
+            vv.back() = val;
+            return;
+        }
+        tt.push_back(now);
+        vv.push_back(val);
+    };
+    while (tok(t)) {
+        const char c = t[0];
+        if (c == '#') {
+            now = strtoull(t.c_str() + 1, nullptr, 10);
+            continue;
+        }
+        if (c == '$') {
+            if (t == "$comment") skip_to_end();
+            continue;   // $dumpvars / $dumpall / $dumpon / $dumpoff / $end
+        }
+        if (c == 'b' || c == 'B') {
+            std::string id;
+            if (!tok(id)) break;
+            auto it = vars.find(id);
+            if (it == vars.end()) continue;
+            std::string bits = t.substr(1);
+            for (const Var &var : it->second) {
+                std::string full = bits;
+                if (full.size() < var.bits.size()) {
+                    const char pad = (full[0] == 'x' || full[0] == 'X') ? 'x' : (full[0] == 'z' || full[0] == 'Z') ? 'z' : '0';
+                    full = std::string(var.bits.size() - full.size(), pad) + full;
+                }
+                const size_t off = full.size() - var.bits.size();
+                for (size_t b = 0; b < var.bits.size(); ++b) {
+                    const uint8_t val = code(full[off + b]);
+                    if (val != 255) put(var.bits[b], val, var.bus);
+                }
+            }
+            continue;
+        }
+        if (c == 'r' || c == 'R') {
+            std::string id;
+            tok(id);
+            continue;
+        }
+        const uint8_t val = code(c);
+        if (val == 255) continue;
+        auto it = vars.find(t.substr(1));
+        if (it == vars.end()) continue;
+        for (const Var &var : it->second)
+            for (size_t k : var.bits) put(k, val, var.bus);
+    }
+    return true;
+}
+
+}  // namespace glsh

@@ -1,0 +1,25 @@
+// VCD stimulus reader and SAIF writer of the gls command-line tools.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace glsh {
+
+// Change lists per bit name.  Scalars keep every change the file lists;
+// bus bits keep only real changes, starting from Z as the reference's bus
+// bit-blasting does (src/VCDParser.cpp:194-242).  A second change of one bit
+// at the same time replaces the first.
+struct VcdData {
+    unsigned time_res = 1;
+    std::string time_unit = "ps";
+    std::unordered_map<std::string, size_t> index;   // bit name -> signal
+    std::vector<std::string> names;
+    std::vector<std::vector<uint64_t>> times;
+    std::vector<std::vector<uint8_t>> values;        // 0, 1=X, 2=Z, 3
+};
+
+bool parse_vcd(const std::string &text, VcdData &v, std::string *err);
+
+}  // namespace glsh
