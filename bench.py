@@ -316,7 +316,7 @@ def gls_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
-                   "seg_events": args.seg or 256},
+                   "seg_events": args.seg or "auto"},
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",

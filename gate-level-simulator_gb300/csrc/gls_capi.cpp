@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <map>
@@ -56,6 +57,8 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->lo = a->hi = 0;
     a->seg_events = ctx->opts.seg_events;
     a->seg_target = (uint32_t)ctx->sm_count * 2048u;
+    a->seg_target_w = ctx->seg_target_w;
+    a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
 }
 
@@ -117,6 +120,16 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         return GLS_ECUDA;
     }
     ctx->def_delay = (uint32_t)(uint64_t)(1.0 * ctx->opts.delay_factor);
+    // tuning knobs: which fan-in classes (bit 0: one input net, 1: two,
+    // 2: three) run warp-per-segment, and how many segments per SM those
+    // classes are cut into
+    if (const char *v = getenv("GLS_SIM_WARP_MASK")) ctx->warp_mask = (uint32_t)strtoul(v, nullptr, 0) & 7u;
+    uint32_t per_sm = 128;
+    if (const char *v = getenv("GLS_SIM_WARP_SEGS")) per_sm = std::max(1u, (uint32_t)strtoul(v, nullptr, 0));
+    ctx->seg_target_w = (uint32_t)ctx->sm_count * per_sm;
+    // testing knob: leave this many unused events after the stimulus, so
+    // that gate outputs sit at large pool offsets (64-bit indexing)
+    if (const char *v = getenv("GLS_POOL_GAP_EVENTS")) ctx->pool_gap = (strtoull(v, nullptr, 0) + 3) & ~3ull;
     *out = ctx;
     return GLS_OK;
 }
@@ -472,7 +485,7 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
             if (cap > limit) cap = std::max<uint64_t>(limit, total + 1024);
         }
     }
-    w->cap = std::max<uint64_t>(std::max<uint64_t>(cap, total + 1024), w->cap);
+    w->cap = std::max<uint64_t>(std::max<uint64_t>(cap, total + 1024) + ctx->pool_gap, w->cap);
     // level scratch: the widest level's fan-in events, estimated from the stimulus
     {
         const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
@@ -539,7 +552,7 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     CK(cudaMemcpyAsync(w->net_off.p, w->init_off.p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "reset offsets");
     CK(cudaMemcpyAsync(w->net_len.p, w->init_len.p, n * 4, cudaMemcpyDeviceToDevice, ctx->stream), "reset lengths");
     CK(cudaMemsetAsync(w->saif.p, 0xFF, n * 24, ctx->stream), "reset saif");
-    unsigned long long small[8] = {w->stim_events, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long small[8] = {w->stim_events + ctx->pool_gap, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(w->small.p, small, sizeof small, cudaMemcpyHostToDevice, ctx->stream), "reset counters");
     WinDev d = make_windev(ctx, w);
     prof_mark(ctx);
@@ -547,13 +560,7 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     ++*launches;
     prof_mark(ctx);
     LevelArgs a;
-    a.meta = ctx->meta.as<DrvMeta>();
-    a.arcs = ctx->arcs.as<ArcDev>();
-    a.ndel = ctx->ndel.as<NetDelay>();
-    a.lut = ctx->lut.as<uint8_t>();
-    a.seg_events = ctx->opts.seg_events;
-    a.seg_target = (uint32_t)ctx->sm_count * 2048u;
-    a.def_delay = ctx->def_delay;
+    ctx_level_args(ctx, &a);
     for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
         a.lo = ctx->drv_level_start[L];
         a.hi = ctx->drv_level_start[L + 1];

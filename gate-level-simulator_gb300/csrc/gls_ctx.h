@@ -89,6 +89,9 @@ struct gls_ctx {
     uint32_t seg_cap = 0;
     uint64_t scr_cap = 0;
     uint32_t def_delay = 1;
+    uint32_t warp_mask = 0;          // fan-in classes run by the warp-per-segment kernel (GLS_SIM_WARP_MASK)
+    uint32_t seg_target_w = 0;       // segments per class for those kernels (GLS_SIM_WARP_SEGS per SM)
+    uint64_t pool_gap = 0;           // unused events between the stimulus and the first gate output (GLS_POOL_GAP_EVENTS)
     std::vector<Window *> windows;
     std::vector<Window *> spare;     // cleared windows whose buffers are reused
     gls_stats stats{};

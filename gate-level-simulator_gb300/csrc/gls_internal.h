@@ -133,7 +133,9 @@ struct LevelArgs {
     const uint8_t *lut;
     uint32_t lo, hi;            // driver range of the level
     uint32_t seg_events;        // fan-in events per segment (0: sized to fill the GPU)
-    uint32_t seg_target;        // segments per level to aim for when seg_events is 0
+    uint32_t seg_target;        // segments per class to aim for (thread-per-segment kernels)
+    uint32_t seg_target_w;      // segments per class to aim for (warp-per-segment kernels)
+    uint32_t warp_mask;         // bit c: fan-in class c runs the warp-per-segment kernel
     uint32_t def_delay;         // delay used when no arc applies
 };
 

@@ -192,7 +192,9 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
         }
         for (int k = 0; k < kClasses; ++k) {
             unsigned long long seg = a.seg_events;
-            if (!seg) seg = max(32ull, (e_cls[k] + a.seg_target - 1) / max(1u, a.seg_target));
+            const bool warp = (a.warp_mask >> k) & 1u;
+            const unsigned long long target = warp ? a.seg_target_w : a.seg_target;
+            if (!seg) seg = max(warp ? 128ull : 32ull, (e_cls[k] + target - 1) / max(1ull, target));
             s_seg[k] = (uint32_t)min(max(seg, floor_seg), 0x7FFFFFFFull);
         }
         s_base = *w.top;
@@ -295,17 +297,17 @@ __device__ __forceinline__ uint32_t sel4(const uint4 &q, uint32_t k)
 // serves four events.  Lists start on a 4-event boundary and their
 // allocations are padded to whole chunks.
 struct Reader {
-    uint32_t cb;        // chunk index of the list start (the list offset / 4)
+    uint64_t cb;        // chunk index of the list start (the list offset / 4; pools pass 2^34 events)
     uint32_t p, e;      // head and end index within the list
     uint4 ct, nt;       // chunk holding the head, next chunk
 
     __device__ __forceinline__ void start(const uint4 *__restrict__ P, uint64_t off, uint32_t p0, uint32_t e0)
     {
-        cb = (uint32_t)(off >> 2);
+        cb = off >> 2;
         p = p0;
         e = e0;
         if (p < e) {
-            const uint32_t c = cb + (p >> 2);
+            const uint64_t c = cb + (p >> 2);
             ct = __ldg(P + c);
             if (((p >> 2) + 1) << 2 < e) nt = __ldg(P + c + 1);
         }
@@ -457,6 +459,477 @@ __global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4)) k_sim(WinD
         const uint32_t S = w.seg_base[i + 1] - sb;
         const DrvMeta md = a.meta[a.lo + i];
         sim_segment<M>(w, a, md, g - sb, S, g, w.scr[i]);
+    }
+}
+
+// ------------------------------------------------------------- warp sim
+// Warp-per-segment kernels for gates with 1, 2 or 3 distinct input nets.
+// A tile is the next kTile fan-in events of the segment in time order,
+// kItems consecutive events per lane; inside a lane the events are walked
+// in order with plain registers, and lanes meet only in a few warp scans
+// per tile (input values before the lane, the candidate suffix minimum,
+// the previous surviving candidate, the push offsets).
+constexpr int kItems = 4;                 // events per lane per tile (more than 3: a step spans at most 2 lanes)
+constexpr int kTile = 32 * kItems;        // events per tile; ring size of every input list
+
+template <int M>
+struct WarpSmem {
+    uint32_t ring[M][kTile];              // the next kTile events of every input list (kInf past its end)
+    uint32_t ab[M == 3 ? kTile : 1];      // 3-input gates: lists 0 and 1 merged
+    uint8_t abj[M == 3 ? kTile : 1];      // and the list each came from
+    uint32_t nd[8 * M];                   // NetDelay of the gate output's input nets
+    uint8_t lut[1 << (2 * M)];            // output value for the input nets' values (2 bits per net)
+};
+
+__device__ __forceinline__ uint32_t tkey(uint32_t word) { return word | 3u; }   // orders by time, kInf stays kInf
+
+// Merge path: positions [d, d + kItems) of the stable merge of two sorted
+// arrays of L entries each (A first on equal times).  Bit k of src tells
+// whether output k came from B, pos[k] its index in the array it came from.
+template <class FA, class FB>
+__device__ __forceinline__ void merge_items(FA A, FB B, uint32_t L, uint32_t d, uint32_t out[kItems], uint32_t &src,
+                                            uint32_t pos[kItems])
+{
+    uint32_t lo = d > L ? d - L : 0u, hi = min(d, L);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (tkey(A(mid)) <= tkey(B(d - 1 - mid))) lo = mid + 1; else hi = mid;
+    }
+    uint32_t i = lo, j = d - lo;
+    uint32_t a = i < L ? A(i) : kInf, b = j < L ? B(j) : kInf;
+    src = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const bool takeb = j < L && (i >= L || tkey(b) < tkey(a));
+        out[k] = takeb ? b : a;
+        pos[k] = takeb ? j : i;
+        if (takeb) {
+            src |= 1u << k;
+            ++j;
+            b = j < L ? B(j) : kInf;
+        } else {
+            ++i;
+            a = i < L ? A(i) : kInf;
+        }
+    }
+}
+
+// regular_delay with the gate's NetDelay entries in shared memory
+template <int M>
+__device__ __forceinline__ uint32_t regular_delay_s(const uint32_t *nd, uint32_t chg, int so, uint32_t curp,
+                                                    uint32_t lastp, uint32_t defd)
+{
+    uint32_t d = kInf;
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        if ((chg >> j) & 1u) {
+            const uint32_t neg = (kNegTab >> (slot_val(lastp, j) * 4 + slot_val(curp, j))) & 1u;
+            d = min(d, nd[j * 8 + neg * 4 + so - 1]);
+        }
+    }
+    return d == kInf ? defd : d;
+}
+
+// One time segment of one gate output, run by a whole warp: the same
+// segment contract as sim_segment (stack region, local stack, min_o).
+//
+// A tile merges the next kTile events of the input lists and keeps those
+// strictly before the time of the last merged one, so that every step (the
+// events of one time, which the reference evaluates once) is whole.  Lane l
+// holds merged events [4l, 4l + 4).  The lanes rebuild the input values
+// after every event, evaluate the cell at the last event of every step,
+// pick the delay, and run the inertial stack in closed form: a candidate
+// survives the tile iff its output time is below every later candidate's,
+// the old stack loses its entries at or after the tile's smallest candidate
+// time, and a survivor is pushed iff its value differs from the previous
+// survivor's (or, for the first, from the stack top).
+template <int M>
+__device__ void sim_segment_warp(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t drv, uint32_t s,
+                                 uint32_t S, uint32_t seg_id, uint64_t scr, WarpSmem<M> &sm)
+{
+    const unsigned FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned lower = (1u << lane) - 1u;
+    const uint32_t *__restrict__ pool = w.pool;
+    // list geometry: lane j < m holds list j, then every lane gets a copy
+    uint64_t myoff = 0;
+    uint32_t mylen = 0;
+    if (lane < md.m) {
+        const uint32_t net = __ldg(&a.meta[drv].net[lane]);
+        myoff = w.net_off[net];
+        mylen = w.net_len[net];
+    }
+    uint64_t off[M];
+    uint32_t len[M];
+    int piv = 0;
+    uint32_t plen = 0;
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        off[j] = __shfl_sync(FULL, myoff, j);
+        len[j] = __shfl_sync(FULL, mylen, j);
+        if (len[j] > plen) { plen = len[j]; piv = j; }
+    }
+    uint64_t poff = 0;
+#pragma unroll
+    for (int j = 0; j < M; ++j) if (j == piv) poff = off[j];
+    const uint32_t plo = (uint32_t)((uint64_t)s * plen / S), phi = (uint32_t)((uint64_t)(s + 1) * plen / S);
+    const uint32_t tlo = s > 0 ? ev_time(__ldg(pool + poff + plo)) : 0u;
+    const uint32_t thi = s + 1 < S ? ev_time(__ldg(pool + poff + phi)) : kInf;
+    uint32_t b = 0, e = 0, vb = kVX;
+    if (lane < md.m) {
+        const uint32_t gl = plen ? (uint32_t)((uint64_t)plo * mylen / plen) : 0u;
+        const uint32_t gh = plen ? (uint32_t)((uint64_t)phi * mylen / plen) : 0u;
+        b = s > 0 ? ((int)lane == piv ? plo : search_from(pool + myoff, mylen, tlo, gl)) : 0u;
+        e = s + 1 < S ? ((int)lane == piv ? phi : search_from(pool + myoff, mylen, thi, gh)) : mylen;
+        if (b > 0) vb = ev_val(__ldg(pool + myoff + b - 1));
+    }
+    uint32_t p[M], E[M];
+    uint32_t region = s, capn = 1, curp_c = 0;
+    bool before = false;
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        p[j] = __shfl_sync(FULL, b, j);
+        E[j] = __shfl_sync(FULL, e, j);
+        curp_c |= __shfl_sync(FULL, vb, j) << (2 * j);
+        region += p[j];
+        capn += E[j] - p[j];
+        before |= p[j] > 0;
+    }
+    uint32_t *ot = w.scratch + scr + region;
+    uint32_t cnt = 0, top = 0, popped_v = kVX;   // stack size, its top word, value of a popped bottom
+    __syncwarp();   // the warp's previous segment is done with the shared tables
+    for (uint32_t k = lane; k < (1u << (2 * M)); k += 32) sm.lut[k] = __ldg(a.lut + md.lut_off + lut_index(k, md));
+    const bool regular = md.flags & kFlagRegular;
+    if (regular && lane < 8u * md.m) sm.nd[lane] = __ldg(&a.ndel[md.dt_off + lane / 8].d[lane % 8]);
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+#pragma unroll
+        for (int r = 0; r < kItems; ++r) {
+            const uint32_t x = p[j] + r * 32 + lane;
+            sm.ring[j][x & (kTile - 1)] = x < E[j] ? __ldg(pool + off[j] + x) : kInf;
+        }
+    }
+    if (s == 0) {
+        top = ev_word(0, kVX);
+        if (lane == 0) ot[0] = top;
+        cnt = 1;
+    }
+    __syncwarp();
+    uint32_t fprev = before ? sm.lut[curp_c] : kVX;
+    uint32_t min_o = kInf;
+    const uint32_t d0 = lane * kItems;
+    for (;;) {
+        // ---- merge: lane holds merged events d0 .. d0+3 and their lists (2 bits each)
+        uint32_t wd[kItems], jsrc = 0;
+        if (M == 1) {
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) wd[k] = sm.ring[0][(p[0] + d0 + k) & (kTile - 1)];
+        } else {
+            const uint32_t *r0 = sm.ring[0], *r1 = sm.ring[1];
+            const uint32_t q0 = p[0], q1 = p[1];
+            auto A0 = [&](uint32_t i) { return r0[(q0 + i) & (kTile - 1)]; };
+            auto A1 = [&](uint32_t i) { return r1[(q1 + i) & (kTile - 1)]; };
+            uint32_t srcb, pos[kItems];
+            if (M == 2) {
+                merge_items(A0, A1, kTile, d0, wd, srcb, pos);
+#pragma unroll
+                for (int k = 0; k < kItems; ++k) jsrc |= ((srcb >> k) & 1u) << (2 * k);
+            } else {
+                uint32_t t01[kItems];
+                merge_items(A0, A1, kTile, d0, t01, srcb, pos);
+#pragma unroll
+                for (int k = 0; k < kItems; ++k) {
+                    sm.ab[d0 + k] = t01[k];
+                    sm.abj[d0 + k] = (uint8_t)((srcb >> k) & 1u);
+                }
+                __syncwarp();
+                const uint32_t *r2 = sm.ring[M - 1];
+                const uint32_t q2 = p[M - 1];
+                auto AB = [&](uint32_t i) { return sm.ab[i]; };
+                auto A2 = [&](uint32_t i) { return r2[(q2 + i) & (kTile - 1)]; };
+                merge_items(AB, A2, kTile, d0, wd, srcb, pos);
+#pragma unroll
+                for (int k = 0; k < kItems; ++k)
+                    jsrc |= (((srcb >> k) & 1u) ? 2u : (uint32_t)sm.abj[pos[k]]) << (2 * k);
+            }
+        }
+        // ---- this tile: the events before the time of the last merged one
+        const uint32_t tc = M == 1 ? kInf : __shfl_sync(FULL, tkey(wd[kItems - 1]), 31);
+        uint32_t vm = 0, cl[M];
+#pragma unroll
+        for (int j = 0; j < M; ++j) cl[j] = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            if (tkey(wd[k]) < tc) {
+                vm |= 1u << k;
+#pragma unroll
+                for (int j = 0; j < M; ++j) cl[j] += ((jsrc >> (2 * k)) & 3u) == (uint32_t)j ? 1u : 0u;
+            }
+        }
+        uint32_t c[M], n = 0;
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+            c[j] = __reduce_add_sync(FULL, cl[j]);
+            n += c[j];
+        }
+        if (n == 0) break;
+        // next events of the lists, stored into the ring after this tile
+        uint32_t nv[M][kItems];
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+#pragma unroll
+            for (int r = 0; r < kItems; ++r) {
+                const uint32_t x = r * 32 + lane, src = p[j] + kTile + x;
+                nv[j][r] = (x < c[j] && src < E[j]) ? __ldg(pool + off[j] + src) : kInf;
+            }
+        }
+        // ---- input values before the lane's first event: the last event of
+        // every list in the lanes before, else the values before the tile
+        uint32_t lv = 0, has = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            if ((vm >> k) & 1u) {
+                const uint32_t J = (jsrc >> (2 * k)) & 3u;
+                lv = (lv & ~(3u << (2 * J))) | (ev_val(wd[k]) << (2 * J));
+                has |= 1u << J;
+            }
+        }
+        uint32_t curp0 = 0;
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+            const unsigned pre = __ballot_sync(FULL, (has >> j) & 1u) & lower;
+            const uint32_t v = __shfl_sync(FULL, lv, pre ? 31 - __clz(pre) : lane);
+            curp0 |= (pre ? slot_val(v, j) : slot_val(curp_c, j)) << (2 * j);
+        }
+        // ---- steps: values after every event; the last event of a step
+        // evaluates the cell with the values before the step and the nets
+        // that changed in it (a step may start in the lane before)
+        uint32_t tt[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) tt[k] = ((vm >> k) & 1u) ? ev_time(wd[k]) : kInf;
+        uint32_t t_next = __shfl_down_sync(FULL, tt[0], 1);
+        if (lane == 31u) t_next = kInf;
+        uint32_t t_prev = __shfl_up_sync(FULL, tt[kItems - 1], 1);
+        if (lane == 0) t_prev = kInf;
+        uint32_t st = curp0, gs = curp0, gc = 0, em = 0, chp = 0, fv = 0;
+        uint32_t cp[kItems], lp[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            cp[k] = 0;
+            lp[k] = 0;
+            if ((vm >> k) & 1u) {
+                const bool newg = tt[k] != (k == 0 ? t_prev : tt[k > 0 ? k - 1 : 0]);
+                if (newg) { gs = st; gc = 0; }
+                const uint32_t J = (jsrc >> (2 * k)) & 3u;
+                st = (st & ~(3u << (2 * J))) | (ev_val(wd[k]) << (2 * J));
+                gc |= 1u << J;
+                cp[k] = st;
+                lp[k] = gs;
+                chp |= gc << (4 * k);
+                if ((k + 1 < kItems ? tt[k + 1 < kItems ? k + 1 : 0] : t_next) != tt[k]) {
+                    em |= 1u << k;
+                    fv |= (uint32_t)sm.lut[st] << (2 * k);
+                }
+            }
+        }
+        {   // a step continued from the lane before: its start values and changed nets come from there
+            const uint32_t in_gs = __shfl_up_sync(FULL, gs, 1);
+            const uint32_t in_gc = __shfl_up_sync(FULL, gc, 1);
+            if ((vm & 1u) && tt[0] == t_prev && em) {
+                const int k1 = __ffs(em) - 1;
+#pragma unroll
+                for (int k = 0; k < kItems; ++k) {
+                    if (k == k1) {
+                        lp[k] = in_gs;
+                        chp |= in_gc << (4 * k);
+                    }
+                }
+            }
+        }
+        const uint32_t lastF = em ? (fv >> (2 * (31 - __clz(em)))) & 3u : 0u;
+        uint32_t fp = __shfl_up_sync(FULL, lastF, 1);
+        if (lane == 0) fp = fprev;
+        // ---- candidates: steps whose output value changes
+        uint32_t o[kItems], am = 0, sov = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            o[k] = kInf;
+            if ((em >> k) & 1u) {
+                const uint32_t F = (fv >> (2 * k)) & 3u;
+                if (F != fp) {
+                    sov |= (uint32_t)((kSenseTab >> (3 * (fp * 4 + F))) & 7u) << (4 * k);
+                    am |= 1u << k;
+                }
+                fp = F;
+            }
+        }
+        bool bad = false;
+        if (regular) {
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                if ((am >> k) & 1u) {
+                    const uint32_t d = regular_delay_s<M>(sm.nd, (chp >> (4 * k)) & 15u, (int)((sov >> (4 * k)) & 15u),
+                                                          cp[k], lp[k], a.def_delay);
+                    o[k] = tt[k] + d;
+                    bad |= o[k] > kMaxTime || o[k] < tt[k];
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                if ((am >> k) & 1u) {
+                    const uint32_t d = select_delay(a.arcs + md.arc_off, md.n_arcs, (chp >> (4 * k)) & 15u,
+                                                    (int)((sov >> (4 * k)) & 15u), cp[k], lp[k], a.def_delay);
+                    o[k] = tt[k] + d;
+                    bad |= o[k] > kMaxTime || o[k] < tt[k];
+                }
+            }
+        }
+        if (__ballot_sync(FULL, bad)) {
+            if (lane == 0) atomicOr(w.err, kErrTime);
+            break;
+        }
+        // ---- inertial stack, src/simulate.cpp:991-1009 in closed form
+        uint32_t later[kItems], sfx = kInf;
+#pragma unroll
+        for (int k = kItems - 1; k >= 0; --k) {
+            later[k] = sfx;
+            sfx = min(sfx, o[k]);
+        }
+        uint32_t x = sfx;   // suffix minimum over the lanes
+#pragma unroll
+        for (int q = 1; q < 32; q <<= 1) {
+            const uint32_t y = __shfl_down_sync(FULL, x, q);
+            if (lane + q < 32u) x = min(x, y);
+        }
+        uint32_t lx = __shfl_down_sync(FULL, x, 1);
+        if (lane == 31u) lx = kInf;
+        const uint32_t tmin = __shfl_sync(FULL, x, 0);
+        if (tmin != kInf) {
+            min_o = min(min_o, tmin);
+            if (cnt > 0 && ev_time(top) >= tmin) {
+                for (;;) {   // drop the stack entries at or after tmin
+                    const uint32_t base = cnt > 32u ? cnt - 32u : 0u;
+                    const uint32_t idx = base + lane;
+                    const uint32_t ent = idx < cnt ? ot[idx] : 0u;
+                    const uint32_t nk = __popc(__ballot_sync(FULL, idx < cnt && ev_time(ent) < tmin));
+                    if (nk > 0) {
+                        cnt = base + nk;
+                        top = __shfl_sync(FULL, ent, nk - 1);
+                        break;
+                    }
+                    if (base == 0) {
+                        popped_v = ev_val(__shfl_sync(FULL, ent, 0));
+                        cnt = 0;
+                        break;
+                    }
+                    cnt = base;
+                }
+            }
+            uint32_t sv = 0;   // survivors
+#pragma unroll
+            for (int k = 0; k < kItems; ++k)
+                if (((am >> k) & 1u) && o[k] < min(later[k], lx)) sv |= 1u << k;
+            const uint32_t lastSF = sv ? (fv >> (2 * (31 - __clz(sv)))) & 3u : 0u;
+            const unsigned pre = __ballot_sync(FULL, sv != 0) & lower;
+            const uint32_t pv = __shfl_sync(FULL, lastSF, pre ? 31 - __clz(pre) : lane);
+            int prevv = pre ? (int)pv : (cnt > 0 ? (int)ev_val(top) : (s == 0 ? (int)popped_v : -1));
+            bool first = pre == 0, emptied = false;
+            uint32_t pm = 0;
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                if ((sv >> k) & 1u) {
+                    const int F = (int)((fv >> (2 * k)) & 3u);
+                    if (F != prevv) pm |= 1u << k;
+                    else if (first && cnt == 0) emptied = true;
+                    first = false;
+                    prevv = F;
+                }
+            }
+            if (__ballot_sync(FULL, emptied)) {
+                if (lane == 0) atomicOr(w.err, kErrEmptied);
+                break;
+            }
+            const uint32_t np = __popc(pm);
+            uint32_t inc = np;
+#pragma unroll
+            for (int q = 1; q < 32; q <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, inc, q);
+                if (lane >= (uint32_t)q) inc += y;
+            }
+            const uint32_t total = __shfl_sync(FULL, inc, 31);
+            if (cnt + total > capn) {
+                if (lane == 0) atomicOr(w.err, kErrRegion);
+                break;
+            }
+            uint32_t wpos = cnt + inc - np, lastw = 0;
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                if ((pm >> k) & 1u) {
+                    lastw = ev_word(o[k], (fv >> (2 * k)) & 3u);
+                    ot[wpos++] = lastw;
+                }
+            }
+            if (total) {
+                top = __shfl_sync(FULL, lastw, 31 - __clz(__ballot_sync(FULL, np > 0)));
+                cnt += total;
+            }
+        }
+        // ---- carry to the next tile, then refill the rings
+        const uint32_t ll = (n - 1) / kItems;
+        curp_c = __shfl_sync(FULL, st, ll);
+        fprev = __shfl_sync(FULL, lastF, ll);
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+#pragma unroll
+            for (int r = 0; r < kItems; ++r) {
+                const uint32_t xr = r * 32 + lane;
+                if (xr < c[j]) sm.ring[j][(p[j] + xr) & (kTile - 1)] = nv[j][r];
+            }
+            p[j] += c[j];
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        SegRec r;
+        r.region = region; r.cnt = cnt; r.min_o = min_o; r.fin = 0;
+        w.segs[seg_id] = r;
+    }
+}
+
+// Warp-per-segment launch for the 1-, 2- and 3-input classes: each block
+// owns a contiguous share of the class's segments and its warps take the
+// next one from a shared counter as they finish.
+template <int M>
+__global__ void __launch_bounds__(128, M == 1 ? 8 : (M == 2 ? 7 : 6)) k_sim_warp(WinDev w, LevelArgs a, uint32_t d0, uint32_t d1)
+{
+    constexpr int kWarps = 4;
+    __shared__ uint32_t s_next;
+    __shared__ WarpSmem<M> sm[kWarps];
+    if (*w.err) return;
+    const uint32_t g0 = w.seg_base[d0], g1 = w.seg_base[d1];
+    const uint32_t total = g1 - g0;
+    const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
+    const uint32_t b0 = g0 + min(total, blockIdx.x * per), b1 = g0 + min(total, (blockIdx.x + 1) * per);
+    if (threadIdx.x == 0) s_next = b0;
+    __syncthreads();
+    const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(&s_next, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= b1) break;
+        uint32_t lo = d0, hi = d1;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (w.seg_base[mid] <= g) lo = mid; else hi = mid;
+        }
+        const uint32_t i = lo;
+        const uint32_t sb = w.seg_base[i];
+        const uint32_t S = w.seg_base[i + 1] - sb;
+        const DrvMeta md = a.meta[a.lo + i];
+        sim_segment_warp<M>(w, a, md, a.lo + i, g - sb, S, g, w.scr[i], sm[wid]);
     }
 }
 
@@ -704,6 +1177,15 @@ void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st)
 
 void launch_sim(const WinDev &w, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count, cudaStream_t st)
 {
+    if ((a.warp_mask >> cls) & 1u) {
+        const int wgrid = sm_count * 8;
+        switch (cls) {
+        case 0: k_sim_warp<1><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
+        case 1: k_sim_warp<2><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
+        case 2: k_sim_warp<3><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
+        default: break;
+        }
+    }
     const int grid = sm_count * (cls <= 1 ? 8 : (cls == 2 ? 6 : 4));
     switch (cls) {
     case 0: k_sim<1><<<grid, 128, 0, st>>>(w, a, d0, d1); break;

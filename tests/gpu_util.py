@@ -2,6 +2,8 @@
 the oracle."""
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from gls.capi import Simulator
@@ -10,9 +12,29 @@ U64 = 2**64 - 1
 U32 = 2**32 - 1
 
 
-def gpu_run(nl, st, t_begin, t_end, calc=0, seg=0, nets=None, pool_events=0):
+def simulator(warp_mask=None, env=None, **kw):
+    """A Simulator; warp_mask picks which fan-in classes (bit 0: one input
+    net, 1: two, 2: three) run the warp-per-segment kernel instead of the
+    thread-per-segment one, env sets other library knobs (both are read when
+    a context is made)."""
+    env = dict(env or {})
+    if warp_mask is not None:
+        env["GLS_SIM_WARP_MASK"] = str(warp_mask)
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        return Simulator(**kw)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+def gpu_run(nl, st, t_begin, t_end, calc=0, seg=0, nets=None, pool_events=0, warp_mask=None, env=None):
     """-> (waves: dict net -> (times, values), saif (n,3) uint64, lengths, stats)."""
-    with Simulator(calc_mode=calc, seg_events=seg, pool_events=pool_events) as s:
+    with simulator(warp_mask, env, calc_mode=calc, seg_events=seg, pool_events=pool_events) as s:
         s.load(nl)
         w = s.add_window(st, t_begin, t_end)
         s.run()

@@ -39,9 +39,12 @@ def test_gpu_matches_golden(idx, seg, gpu):
         assert gs[int(net)].tolist() == rec, f"{r['label']}: SAIF net {net}"
 
 
+@pytest.mark.parametrize("mask", [7, 0])
 @pytest.mark.parametrize("seg", [8, 13, 256])
 @pytest.mark.parametrize("seed", range(16))
-def test_gpu_random_vs_oracle(seed, seg, gpu, oracle_bin):
+def test_gpu_random_vs_oracle(seed, seg, mask, gpu, oracle_bin):
+    """Random small designs; mask 7 runs the 1-3 input gates warp-per-segment,
+    mask 0 thread-per-segment."""
     nl, st = random_case(seed, max_gates=16, max_in=6, horizon=600, max_events=80,
                          zero_delay=(seed % 5 == 0))
     calc = "literal" if seed % 4 == 3 else "fixed"
@@ -49,8 +52,9 @@ def test_gpu_random_vs_oracle(seed, seg, gpu, oracle_bin):
         ow, osaif, _ = run_oracle(nl, st, 0, 700, calc=calc)
     except Exception:
         pytest.skip("oracle rejects this case (zero delay at time 0)")
-    gw, gs, _, _ = gpu_run(nl, st, 0, 700, calc=CALC_LITERAL if calc == "literal" else CALC_FIXED, seg=seg)
-    assert_same(gw, gs, ow, osaif, f"seed {seed} seg {seg}")
+    gw, gs, _, _ = gpu_run(nl, st, 0, 700, calc=CALC_LITERAL if calc == "literal" else CALC_FIXED, seg=seg,
+                           warp_mask=mask)
+    assert_same(gw, gs, ow, osaif, f"seed {seed} seg {seg} mask {mask}")
 
 
 @pytest.mark.parametrize("seed", range(4))
@@ -58,9 +62,22 @@ def test_gpu_dense_random_vs_oracle(seed, gpu, oracle_bin):
     """Many gates and long lists: every level has several segments per gate."""
     nl, st = random_case(900 + seed, max_gates=120, max_in=8, horizon=20000, max_events=2000, xz=seed % 2 == 0)
     ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
-    for seg in (16, 512):
-        gw, gs, _, _ = gpu_run(nl, st, 100, 15000, seg=seg)
-        assert_same(gw, gs, ow, osaif, f"dense seed {seed} seg {seg}")
+    for seg, mask in ((16, 7), (512, 7), (200, 0), (0, 7), (0, 0)):
+        gw, gs, _, _ = gpu_run(nl, st, 100, 15000, seg=seg, warp_mask=mask)
+        assert_same(gw, gs, ow, osaif, f"dense seed {seed} seg {seg} mask {mask}")
+
+
+def test_gpu_pool_offsets_past_2_34_events(gpu, oracle_bin):
+    """Gate outputs placed past 2^34 events (64 GiB) into the pool: list
+    offsets and 16-byte chunk indexes need 64 bits there (the full large
+    configuration's pool reaches 4.2e10 events)."""
+    nl, st = random_case(950, max_gates=120, max_in=8, horizon=20000, max_events=2000)
+    ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
+    gap = {"GLS_POOL_GAP_EVENTS": str((1 << 34) + 4)}
+    for seg, mask in ((16, 0), (0, 0), (0, 7)):
+        gw, gs, _, stats = gpu_run(nl, st, 100, 15000, seg=seg, warp_mask=mask, env=gap)
+        assert stats["pool_events"] > 1 << 34
+        assert_same(gw, gs, ow, osaif, f"gap seg {seg} mask {mask}")
 
 
 def test_gpu_c1_full_config(gpu, oracle_bin):
