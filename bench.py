@@ -229,7 +229,12 @@ def gls_arm(args):
     cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
     # replicas: every rank simulates its own independent window (weak scaling)
     st = stimulus_for(cfg, nl, args.seed + 1 + 1000 * rank)
-    sim = Simulator(device=local, stream=stream.cuda_stream, profile=True, seg_events=args.seg)
+    from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED
+    alloc = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}[args.alloc]
+    sim = Simulator(device=local, stream=stream.cuda_stream, profile=True, seg_events=args.seg, alloc_mode=alloc)
+    if args.alloc == "learned":
+        from gls import presize
+        sim.set_presize_model(presize.load(args.model or presize.DEFAULT_MODEL))
     sim.load(nl)
     w = sim.add_window(st, 0, cfg.t_end)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
@@ -316,7 +321,7 @@ def gls_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
-                   "seg_events": args.seg or "auto"},
+                   "seg_events": args.seg or "auto", "alloc": args.alloc},
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -362,6 +367,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--seg", type=int, default=0, help="fan-in events per time segment (0 = library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--alloc", default="bound", choices=["bound", "exact", "learned"],
+                    help="gate-output slot allocation: upper bound, exact, or learned presize")
+    ap.add_argument("--model", default=None, help="presize model (.npz) for --alloc learned")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling cases)")
     ap.add_argument("--depth", type=int, default=None, help="override the logic depth (profiling cases)")
     ap.add_argument("--cycles", type=int, default=None, help="override the cycle count (profiling cases)")

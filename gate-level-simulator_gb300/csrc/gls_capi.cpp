@@ -19,6 +19,7 @@
 #include "gls.h"
 #include "gls_internal.h"
 #include "gls_ctx.h"
+#include "gls_presize.h"
 
 using namespace gls;
 
@@ -60,6 +61,8 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->seg_target_w = ctx->seg_target_w;
     a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
+    a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
+    a->pred = ctx->pred.as<uint32_t>();
 }
 
 namespace {
@@ -94,7 +97,8 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         ctx->opts.delay_factor = 1.0;
     }
     if (ctx->opts.delay_factor <= 0.0) ctx->opts.delay_factor = 1.0;
-    if (ctx->opts.calc_mode != GLS_CALC_FIXED && ctx->opts.calc_mode != GLS_CALC_LITERAL) {
+    if ((ctx->opts.calc_mode != GLS_CALC_FIXED && ctx->opts.calc_mode != GLS_CALC_LITERAL) ||
+        ctx->opts.alloc_mode < GLS_ALLOC_BOUND || ctx->opts.alloc_mode > GLS_ALLOC_LEARNED) {
         delete ctx;
         return GLS_EINVAL;
     }
@@ -199,6 +203,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     ctx->cls_start.clear();
     ctx->pins_total = 0;
     std::vector<uint8_t> consumed(nl->n_nets, 0);
+    std::vector<uint32_t> fanout(nl->n_nets, 0), cell_of_net(nl->n_nets, 0xFFFFFFFFu);
     for (uint32_t L = 0; L < nl->n_levels; ++L) {
         for (uint32_t i = nl->level_start[L]; i < nl->level_start[L + 1]; ++i) {
             const uint32_t cid = nl->inst_cell[i];
@@ -216,6 +221,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
                 const uint32_t net = pins[p];
                 if (net >= nl->n_nets) return fail(ctx, GLS_EINVAL, "instance %u: bad net", i);
                 consumed[net] = 1;
+                ++fanout[net];
                 int slotp = -1;
                 for (int j = 0; j < m; ++j) if (md.net[j] == net) slotp = j;
                 if (slotp < 0) {
@@ -239,6 +245,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
                 if (onet >= nl->n_nets) return fail(ctx, GLS_EINVAL, "instance %u: bad output net", i);
                 if (drv_level_of_net[onet] >= 0) return fail(ctx, GLS_EINVAL, "net %u has two drivers", onet);
                 drv_level_of_net[onet] = (int32_t)L;
+                cell_of_net[onet] = cid;
                 d.out_net = onet;
                 if (o == 0) d.flags |= kFlagFirstOut;
                 auto key = std::make_pair(cid, o);
@@ -340,6 +347,49 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     if (h_ndel.empty()) h_ndel.push_back(NetDelay{{kInf, kInf, kInf, kInf, kInf, kInf, kInf, kInf}});
     if (h_lut.empty()) h_lut.push_back(kVX);
     if (h_meta.empty()) h_meta.push_back(DrvMeta{});
+    // static presize features per gate output (feature order in gls.h)
+    std::vector<float> h_feat(h_meta.size() * kIn, 0.f);
+    for (size_t d = 0; d < ctx->n_drv; ++d) {
+        const DrvMeta &md = h_meta[d];
+        float *f = &h_feat[d * kIn];
+        const uint32_t cid = cell_of_net[md.out_net];
+        if (cid < 13) f[cid] = 1.f;
+        f[13] = md.n_pins / 6.f;
+        f[14] = md.m / 6.f;
+        double sr = 0, sf = 0;
+        uint32_t mn = 0xFFFFFFFFu, mx = 0;
+        for (uint32_t k = 0; k < md.n_arcs; ++k) {
+            const ArcDev &A = h_arcs[md.arc_off + k];
+            sr += A.rise;
+            sf += A.fall;
+            mn = std::min(mn, std::min(A.rise, A.fall));
+            mx = std::max(mx, std::max(A.rise, A.fall));
+        }
+        const double na = md.n_arcs ? md.n_arcs : 1;
+        if (!md.n_arcs) { sr = sf = ctx->def_delay; mn = mx = ctx->def_delay; }
+        f[24] = (float)(sr / na / 100.0);
+        f[25] = (float)(sf / na / 100.0);
+        f[26] = (float)(mn / 100.0);
+        f[27] = (float)(mx / 100.0);
+        f[28] = (float)(std::log1p((double)fanout[md.out_net]) / 6.0);
+        // share of single-input changes (0 <-> 1) that change the output
+        const uint8_t *lut = &h_lut[md.lut_off];
+        uint32_t changes = 0, trials = 0;
+        for (uint32_t c = 0; c < (1u << md.n_pins); ++c) {
+            uint32_t idx = 0;
+            for (int p = 0; p < md.n_pins; ++p) idx |= (((c >> p) & 1u) ? 3u : 0u) << (2 * p);
+            for (int p = 0; p < md.n_pins; ++p) {
+                changes += lut[idx] != lut[idx ^ (3u << (2 * p))];
+                ++trials;
+            }
+        }
+        f[29] = trials ? (float)changes / trials : 0.f;
+        f[30] = (md.flags & kFlagRegular) ? 1.f : 0.f;
+        f[31] = 1.f;
+    }
+    CK(ctx->feat_static.ensure(h_feat.size() * 4), "alloc presize features");
+    CK(cudaMemcpy(ctx->feat_static.p, h_feat.data(), h_feat.size() * 4, cudaMemcpyHostToDevice),
+       "upload presize features");
     CK(ctx->meta.ensure(h_meta.size() * sizeof(DrvMeta)), "alloc meta");
     CK(ctx->arcs.ensure(h_arcs.size() * sizeof(ArcDev)), "alloc arcs");
     CK(ctx->ndel.ensure(h_ndel.size() * sizeof(NetDelay)), "alloc net delays");
@@ -352,6 +402,8 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     CK(ctx->seg_base.ensure((size_t)(ctx->max_width + 1) * 4), "alloc seg_base");
     CK(ctx->slot.ensure((size_t)(ctx->max_width + 1) * 8), "alloc slot");
     CK(ctx->scr.ensure((size_t)(ctx->max_width + 1) * 8), "alloc scratch offsets");
+    CK(ctx->res.ensure((size_t)(ctx->max_width + 1) * 4), "alloc reserved lengths");
+    CK(ctx->pred.ensure((size_t)(ctx->max_width + 1) * 4), "alloc presize predictions");
     ctx->seg_cap = std::max<uint32_t>(1u << 21, 8 * ctx->max_width + 64);
     CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "alloc segs");
     CK(ctx->copies.ensure((size_t)ctx->seg_cap * sizeof(CopyRec)), "alloc copies");
@@ -514,6 +566,8 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     d.counters = sm + 1;     // 4 counters
     d.err = reinterpret_cast<uint32_t *>(sm + 5);
     d.n_segs = reinterpret_cast<uint32_t *>(sm + 6);
+    d.n_over = sm + 7;
+    d.res = ctx->res.as<uint32_t>();
     d.seg_base = ctx->seg_base.as<uint32_t>();
     d.slot = ctx->slot.as<uint64_t>();
     d.scr = ctx->scr.as<uint64_t>();
@@ -565,6 +619,19 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
         a.lo = ctx->drv_level_start[L];
         a.hi = ctx->drv_level_start[L + 1];
         if (a.hi == a.lo) continue;
+        if (a.alloc_mode == kAllocLearned) {
+            // the level's presize predictions (tensor cores) before its slots are planned
+            PresizeArgs pa;
+            ctx_presize_args(ctx, &pa);
+            pa.net_len = d.net_len;
+            pa.saif = d.saif;
+            pa.lo = a.lo;
+            pa.n = a.hi - a.lo;
+            pa.pred = ctx->pred.as<uint32_t>();
+            pa.err = d.err;
+            launch_presize(pa, true, ctx->stream);
+            ++*launches;
+        }
         launch_plan(d, a, ctx->stream);
         prof_mark(ctx);
         for (int c = 0; c < kClasses; ++c) {
@@ -588,6 +655,8 @@ extern "C" int gls_run(gls_ctx *ctx)
 {
     if (!ctx) return GLS_EINVAL;
     if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "run before load_netlist");
+    if (ctx->opts.alloc_mode == GLS_ALLOC_LEARNED && !ctx->have_model)
+        return fail(ctx, GLS_ESTATE, "GLS_ALLOC_LEARNED needs gls_set_presize_model before gls_run");
     cudaSetDevice(ctx->opts.device);
     uint32_t launches = 0;
     ctx->prof_used = 0;
@@ -623,7 +692,7 @@ extern "C" int gls_run(gls_ctx *ctx)
             }
         }
     }
-    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0;
+    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0, over_ev = 0;
     // check every window; regrow the pool or the segment table and rerun
     for (Window *w : ctx->windows) {
         for (int attempt = 0;; ++attempt) {
@@ -631,6 +700,7 @@ extern "C" int gls_run(gls_ctx *ctx)
             CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
             const uint32_t err = (uint32_t)small[5];
             if (!err) {
+                over_ev += small[7];
                 gate_ev += small[1];
                 out_ev += small[2];
                 segs += small[3];
@@ -639,6 +709,7 @@ extern "C" int gls_run(gls_ctx *ctx)
                 pool_bytes += w->cap * 4;
                 break;
             }
+            if (err & kErrPresize) return fail(ctx, GLS_ECUDA, "presize kernel timed out waiting for its tensor-core MMA");
             if (err & (kErrRegion | kErrEmptied | kErrTime)) {
                 return fail(ctx, err & kErrTime ? GLS_ERANGE : GLS_EINVAL,
                             "simulation error flags 0x%x (%s)", err,
@@ -690,6 +761,8 @@ extern "C" int gls_run(gls_ctx *ctx)
     ctx->stats.sim_ms = kms[2];
     ctx->stats.combine_ms = kms[3];
     ctx->stats.fanin_bytes = fanin_ev * 5;
+    ctx->stats.presize_overflows = over_ev;
+    ctx->stats.pool_used = pool_ev;
     return GLS_OK;
 }
 

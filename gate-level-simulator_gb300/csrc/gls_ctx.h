@@ -92,6 +92,14 @@ struct gls_ctx {
     uint32_t warp_mask = 0;          // fan-in classes run by the warp-per-segment kernel (GLS_SIM_WARP_MASK)
     uint32_t seg_target_w = 0;       // segments per class for those kernels (GLS_SIM_WARP_SEGS per SM)
     uint64_t pool_gap = 0;           // unused events between the stimulus and the first gate output (GLS_POOL_GAP_EVENTS)
+    // learned presize (GLS_ALLOC_LEARNED)
+    DevBuf feat_static;              // per driver x 32 static features
+    DevBuf pred, res;                // per driver of the widest level: predicted / reserved events
+    DevBuf mlp_params, mlp_img;      // FP32 parameters and the BF16 weight image
+    DevBuf aux;                      // small device scratch of the presize calls (error word)
+    bool have_model = false;
+    float margin = 0.f;
+    uint32_t slack = 0;
     std::vector<Window *> windows;
     std::vector<Window *> spare;     // cleared windows whose buffers are reused
     gls_stats stats{};
@@ -105,3 +113,6 @@ struct gls_ctx {
 int ctx_fail(gls_ctx *c, int code, const char *fmt, ...);
 // The per-level kernel arguments that do not depend on the level.
 void ctx_level_args(const gls_ctx *ctx, gls::LevelArgs *a);
+namespace gls { struct PresizeArgs; }
+// The presize-kernel arguments of the installed model (rows, range and outputs left empty).
+void ctx_presize_args(const gls_ctx *ctx, gls::PresizeArgs *a);

@@ -35,6 +35,12 @@ constexpr uint32_t kErrEmptied = 4u;    // output list emptied (zero delay at t=
 constexpr uint32_t kErrSegCap = 8u;     // segment table too small
 constexpr uint32_t kErrTime = 16u;      // an output time passed kMaxTime
 constexpr uint32_t kErrScratch = 32u;   // level scratch exhausted
+constexpr uint32_t kErrPresize = 64u;   // the tensor-core presize kernel gave up waiting for its MMA
+
+// output slot allocation (GLS_ALLOC_*): an upper bound reserved before the
+// level runs; the exact length once the level's stacks are linked; or a
+// predicted length, with the exact placement for gates that outgrow it
+constexpr uint32_t kAllocBound = 0, kAllocExact = 1, kAllocLearned = 2;
 
 constexpr uint8_t kFlagIdent = 1;    // slot p feeds pin p for every pin
 constexpr uint8_t kFlagRegular = 2;  // every input net has no arc, one both-edge arc, or a posedge/negedge pair
@@ -97,7 +103,7 @@ struct SegRec {             // one time segment of one gate output
 
 struct CopyRec {            // what k_copy does for one segment
     uint64_t src;           // scratch index of the first kept entry
-    uint64_t dst;           // pool index it goes to
+    uint64_t dst;           // position of that entry in the gate output's list
     uint32_t n;             // entries to copy
     uint32_t drv;           // gate output (level-relative)
     unsigned long long cprev;  // clamped time of the final event before this segment's first
@@ -119,6 +125,8 @@ struct WinDev {
     SegRec *segs;
     CopyRec *copies;            // per segment, written by k_link
     uint32_t *n_segs;
+    uint32_t *res;              // per driver of the level: events reserved in its slot (exact / learned modes)
+    unsigned long long *n_over; // gate outputs placed exactly because the presize was short (learned mode)
     uint32_t *scratch;          // level scratch: segment stacks (event words)
     uint64_t cap;               // pool capacity (events)
     uint64_t scr_cap;           // scratch capacity (events)
@@ -137,6 +145,8 @@ struct LevelArgs {
     uint32_t seg_target_w;      // segments per class to aim for (warp-per-segment kernels)
     uint32_t warp_mask;         // bit c: fan-in class c runs the warp-per-segment kernel
     uint32_t def_delay;         // delay used when no arc applies
+    uint32_t alloc_mode;        // kAllocBound / kAllocExact / kAllocLearned
+    const uint32_t *pred;       // learned mode: predicted slot length per driver of the level
 };
 
 // fan-in class of a gate output by its number of distinct input nets

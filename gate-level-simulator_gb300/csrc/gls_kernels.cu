@@ -217,6 +217,9 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
             const uint32_t seg = s_seg[fanin_class(md.m)];
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
             slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
+            if (a.alloc_mode == kAllocExact) slot = 0;
+            else if (a.alloc_mode == kAllocLearned) slot = min(slot, ((unsigned long long)a.pred[i] + 3) & ~3ull);
+            if (a.alloc_mode != kAllocBound) w.res[i] = (uint32_t)slot;
             scr = (E + S + 3) & ~3ull;      // segment stacks: events of the segment (+1 for the first)
         }
         uint32_t tS;
@@ -1029,7 +1032,7 @@ __global__ void __launch_bounds__(256) k_link(WinDev w, LevelArgs a)
         if (valid) {
             CopyRec c;
             c.src = scr + region + drop;
-            c.dst = slot + pos;
+            c.dst = pos;
             c.n = fin;
             c.drv = i;
             c.cprev = fprior ? csh : cprev;
@@ -1046,6 +1049,19 @@ __global__ void __launch_bounds__(256) k_link(WinDev w, LevelArgs a)
         carry_pos += __shfl_sync(FULL, inc, 31);
     }
     if (lane == 0) {
+        if (a.alloc_mode != kAllocBound) {
+            // exact placement now that the length is known (every gate in
+            // exact mode, gates that outgrew their predicted slot in learned mode)
+            uint64_t st = slot;
+            if (a.alloc_mode == kAllocExact || carry_pos > w.res[i]) {
+                const unsigned long long need = (carry_pos + 3ull) & ~3ull;
+                st = atomicAdd(w.top, need);
+                if (st + need > w.cap) atomicOr(w.err, kErrPool);
+                if (a.alloc_mode == kAllocLearned) atomicAdd(w.n_over, 1ull);
+                w.slot[i] = st;
+            }
+            w.net_off[out_net] = st;
+        }
         // the last event holds until t_end; k_copy adds the rest
         unsigned long long acc[3] = {0, 0, 0};
         saif_add(acc, pclass, w.t_end - cprev);
@@ -1110,13 +1126,14 @@ __global__ void __launch_bounds__(256) k_copy(WinDev w, LevelArgs a)
         uint32_t nmax = n;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
+        const uint64_t dst = live ? w.slot[c.drv] + c.dst : 0;
         for (uint32_t i0 = 0; i0 < nmax; i0 += W) {
             const uint32_t i = i0 + sub;
             const bool v = i < n;
             uint32_t word = 0;
             if (v) {
                 word = w.scratch[c.src + i];
-                w.pool[c.dst + i] = word;
+                w.pool[dst + i] = word;
             }
             integrate_group<W>(w, word, v, i0 < n ? n - i0 : 1u, i0 < n, cprev, pclass, acc);
         }

@@ -115,6 +115,8 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     d.counters = small + 1;
     d.err = reinterpret_cast<uint32_t *>(small + 5);
     d.n_segs = reinterpret_cast<uint32_t *>(small + 6);
+    d.n_over = small + 7;
+    d.res = nullptr;
     d.seg_base = reinterpret_cast<uint32_t *>(base + kOffSegBase);
     d.slot = reinterpret_cast<uint64_t *>(base + kOffSlot);
     d.scr = reinterpret_cast<uint64_t *>(base + kOffScr);
@@ -128,6 +130,8 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     d.t_end = t_end;
     LevelArgs a;
     ctx_level_args(ctx, &a);
+    a.alloc_mode = kAllocBound;   // the caller's pool: slots reserved up front
+    a.pred = nullptr;
     a.lo = lo + first;
     a.hi = a.lo + count;
     launch_plan(d, a, ctx->stream);

@@ -18,12 +18,17 @@ LIB_PATH = Path(__file__).resolve().parent.parent / "lib" / "libgls.so"
 
 GLS_OK, GLS_EINVAL, GLS_ECUDA, GLS_ENOMEM, GLS_ESTATE, GLS_ERANGE, GLS_EOVERFLOW = range(7)
 CALC_FIXED, CALC_LITERAL = 0, 1
-ALLOC_BOUND, ALLOC_EXACT = 0, 1
+ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED = 0, 1, 2
+MLP_IN, MLP_HID = 32, 128
+MLP_PARAMS = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_HID + 1
 
 # every symbol include/gls.h declares
 EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "gls_add_window",
             "gls_clear_windows", "gls_run", "gls_saif_counts", "gls_waveform_lengths", "gls_waveform",
-            "gls_stats_get", "gls_cell_lut", "gls_abi_version", "gls_run_level_static"]
+            "gls_stats_get", "gls_cell_lut", "gls_abi_version", "gls_run_level_static",
+            "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
+            "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
+            "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params"]
 
 
 class GlsError(RuntimeError):
@@ -56,10 +61,31 @@ class Stats(C.Structure):
                 ("pool_events", C.c_uint64), ("pool_bytes", C.c_uint64), ("overflow_retries", C.c_uint64),
                 ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("n_windows", C.c_uint32),
                 ("plan_ms", C.c_double), ("sim_ms", C.c_double), ("combine_ms", C.c_double),
-                ("stim_ms", C.c_double), ("fanin_bytes", C.c_uint64)]
+                ("stim_ms", C.c_double), ("fanin_bytes", C.c_uint64), ("presize_overflows", C.c_uint64),
+                ("pool_used", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PresizeModel(C.Structure):
+    _fields_ = [("params", C.c_float * MLP_PARAMS), ("margin", C.c_float), ("slack", C.c_uint32)]
+
+
+class TrainOpts(C.Structure):
+    _fields_ = [("batch", C.c_uint32), ("epochs", C.c_uint32), ("lr", C.c_float), ("huber", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+def presize_model(params: np.ndarray, margin: float = 0.25, slack: int = 8) -> PresizeModel:
+    m = PresizeModel()
+    p = np.ascontiguousarray(params, np.float32)
+    if p.shape != (MLP_PARAMS,):
+        raise ValueError(f"presize parameters: {MLP_PARAMS} floats expected, got {p.shape}")
+    C.memmove(m.params, p.ctypes.data, p.nbytes)
+    m.margin = margin
+    m.slack = slack
+    return m
 
 
 _lib = None
@@ -92,6 +118,20 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_abi_version.restype = C.c_int
     lib.gls_run_level_static.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]
+    lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
+    lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
+                                        C.POINTER(C.c_uint64)]
+    lib.gls_presize_predict.argtypes = [C.c_void_p, C.POINTER(PresizeModel), C.c_void_p, C.c_uint64, C.c_void_p,
+                                        C.c_int]
+    lib.gls_trainer_create.argtypes = [C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]
+    lib.gls_trainer_destroy.argtypes = [C.c_void_p]
+    lib.gls_trainer_error.restype = C.c_char_p
+    lib.gls_trainer_error.argtypes = [C.c_void_p]
+    lib.gls_trainer_set_data.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]
+    lib.gls_trainer_fit.argtypes = [C.c_void_p, C.POINTER(TrainOpts), C.c_void_p]
+    lib.gls_trainer_grad.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_float, C.c_void_p, C.c_void_p]
+    lib.gls_trainer_get_params.argtypes = [C.c_void_p, C.c_void_p]
+    lib.gls_trainer_set_params.argtypes = [C.c_void_p, C.c_void_p]
     if path is None:
         _lib = lib
     return lib
@@ -223,3 +263,88 @@ class Simulator:
         s = Stats()
         self._check(self.lib.gls_stats_get(self.h, C.byref(s)), "stats")
         return s.as_dict()
+
+    # ---------------------------------------------------------- presize
+    def set_presize_model(self, params: np.ndarray, margin: float = 0.25, slack: int = 8):
+        """Install the MLP used by ALLOC_LEARNED (FP32 parameters, flat)."""
+        self._model = presize_model(params, margin, slack)
+        self._check(self.lib.gls_set_presize_model(self.h, C.byref(self._model)), "set_presize_model")
+
+    def presize_samples(self, window: int = 0):
+        """(features (n, 32) float32, output-list lengths (n,) uint32) of every gate output."""
+        n = C.c_uint64()
+        self._check(self.lib.gls_presize_samples(self.h, window, None, None, 0, C.byref(n)), "presize_samples")
+        feat = np.zeros((n.value, MLP_IN), np.float32)
+        cnt = np.zeros(n.value, np.uint32)
+        self._check(self.lib.gls_presize_samples(self.h, window, _ptr(feat), _ptr(cnt), n.value, C.byref(n)),
+                    "presize_samples")
+        return feat, cnt
+
+    def presize_predict(self, params: np.ndarray, feat: np.ndarray, tensor_cores: bool = True) -> np.ndarray:
+        """Network output y for host feature rows (tensor-core or FP32 kernel)."""
+        m = presize_model(params)
+        f = np.ascontiguousarray(feat, np.float32)
+        y = np.zeros(len(f), np.float32)
+        self._check(self.lib.gls_presize_predict(self.h, C.byref(m), _ptr(f), len(f), _ptr(y),
+                                                 1 if tensor_cores else 0), "presize_predict")
+        return y
+
+
+class Trainer:
+    """GPU training of the presize MLP (FP32, Adam, Huber loss on log lengths)."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.gls_trainer_create(device, seed, C.byref(h))
+        if rc:
+            raise GlsError(rc, "gls_trainer_create failed (no CUDA device?)")
+        self.h = h
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise GlsError(rc, f"{what}: {self.lib.gls_trainer_error(self.h).decode()}")
+
+    def close(self):
+        if self.h:
+            self.lib.gls_trainer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_data(self, feat: np.ndarray, target: np.ndarray):
+        self._feat = np.ascontiguousarray(feat, np.float32)
+        self._target = np.ascontiguousarray(target, np.float32)
+        self._check(self.lib.gls_trainer_set_data(self.h, _ptr(self._feat), _ptr(self._target), len(self._target)),
+                    "set_data")
+
+    def fit(self, epochs: int, batch: int = 8192, lr: float = 1e-3, huber: float = 1.0, seed: int = 0) -> np.ndarray:
+        loss = np.zeros(epochs, np.float32)
+        o = TrainOpts(batch, epochs, lr, huber, seed)
+        self._check(self.lib.gls_trainer_fit(self.h, C.byref(o), _ptr(loss)), "fit")
+        return loss
+
+    def grad(self, first: int, n: int, huber: float = 1.0):
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._check(self.lib.gls_trainer_grad(self.h, first, n, huber, _ptr(g), _ptr(loss)), "grad")
+        return g, float(loss[0])
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(MLP_PARAMS, np.float32)
+        self._check(self.lib.gls_trainer_get_params(self.h, _ptr(p)), "get_params")
+        return p
+
+    def set_params(self, p: np.ndarray):
+        self._p = np.ascontiguousarray(p, np.float32)
+        self._check(self.lib.gls_trainer_set_params(self.h, _ptr(self._p)), "set_params")

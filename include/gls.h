@@ -47,8 +47,10 @@ extern "C" {
 #define GLS_CALC_LITERAL 1  /* the shipped calc of src/simulate.cpp:382-870 */
 
 /* output allocation modes */
-#define GLS_ALLOC_BOUND 0   /* slot per gate = sum of fan-in events + segments */
-#define GLS_ALLOC_EXACT 1   /* count in scratch, then copy to exact-size lists */
+#define GLS_ALLOC_BOUND 0   /* slot per gate output reserved up front: its fan-in events + 1 */
+#define GLS_ALLOC_EXACT 1   /* count-then-fill: a list is placed once its final length is known */
+#define GLS_ALLOC_LEARNED 2 /* slot presized by the presize model (gls_set_presize_model); an
+                               output that outgrows its slot is placed exactly instead */
 
 /* primitive ids of the reference function program (src/PreProcess.cpp:1194-1197) */
 #define GLS_F_AND 0
@@ -143,6 +145,8 @@ typedef struct {
     /* with opts.profile: device time per kernel class in the last gls_run */
     double plan_ms, sim_ms, combine_ms, stim_ms;
     uint64_t fanin_bytes;     /* fan-in event bytes the gate kernels read (5 B per event per net) */
+    uint64_t presize_overflows; /* GLS_ALLOC_LEARNED: gate outputs longer than their predicted slot */
+    uint64_t pool_used;       /* events allocated in the pool (stimulus + gate-output slots) */
 } gls_stats;
 
 /* Create a context on opts->device.  Replaces cudaSetDevice(0) and the
@@ -190,6 +194,80 @@ int gls_cell_lut(const gls_cell *cell, const gls_prim *prims, int out,
                  int calc_mode, uint8_t *lut, uint32_t lut_cap);
 
 int gls_abi_version(void);
+
+/* ---------------------------------------------------------------------
+ * Learned presize.  No counterpart in the reference, which sizes every
+ * gate output from its fan-in rows (src/simulate.cu:2300-2306) and then
+ * compacts (src/simulate.cu:1104-1357).
+ *
+ * A multilayer perceptron 32 -> 128 -> 128 -> 1 (ReLU) maps a gate
+ * output's features to y ~ log(1 + length of its output list).  Features,
+ * in order: 0-12 one-hot cell index (cells 0..12 of the netlist); 13 input
+ * pins / 6; 14 distinct input nets / 6; 15-17 log(1 + events) of input nets
+ * 0-2 / 12; 18 log(1 + sum of input events) / 12; 19 log(1 + max) / 12;
+ * 20 log(1 + min) / 12; 21 log(1 + expected output changes) / 12, where
+ * every input change counts with the probability that the other inputs
+ * sensitize the output to it (truth table, inputs independent, each at 1
+ * for its SAIF share T1 / (T0 + T1)); 22 the probability that the output is
+ * 1 under the same assumption; 23 the mean 1-share of the inputs; 24 mean rise, 25 mean fall, 26 min, 27 max arc delay
+ * (time units / 100); 28 log(1 + fan-out) / 6; 29 the fraction of single
+ * input changes that change the output (from the truth table); 30 1 when
+ * every input net has a simple arc set; 31 constant 1.
+ * In GLS_ALLOC_LEARNED mode every level first runs the network on the
+ * tensor cores (BF16 operands, FP32 accumulation) and reserves
+ *   min(fan-in events + 1, ceil((exp(y) - 1) * (1 + margin)) + slack)
+ * events per gate output.
+ * --------------------------------------------------------------------- */
+#define GLS_MLP_IN 32
+#define GLS_MLP_HID 128
+#define GLS_MLP_PARAMS (GLS_MLP_HID * GLS_MLP_IN + GLS_MLP_HID + GLS_MLP_HID * GLS_MLP_HID + GLS_MLP_HID + GLS_MLP_HID + 1)
+
+typedef struct {
+    /* FP32 parameters in this order: w1[128][32], b1[128], w2[128][128],
+     * b2[128], w3[128], b3 (row = output unit).  Inference rounds w1 and w2
+     * to BF16. */
+    float params[GLS_MLP_PARAMS];
+    float margin;      /* relative slack on the predicted length */
+    uint32_t slack;    /* absolute slack, events */
+} gls_presize_model;
+
+/* Install the model used by GLS_ALLOC_LEARNED (copied). */
+int gls_set_presize_model(gls_ctx *ctx, const gls_presize_model *model);
+
+/* Training pairs from a finished window: for every gate output (the
+ * library's driver order) its 32 features as the learned mode computes them
+ * and the length of its output list.  feat holds cap x 32 floats, count cap
+ * entries; *n receives the number of gate outputs. */
+int gls_presize_samples(gls_ctx *ctx, uint32_t window, float *feat, uint32_t *count, uint64_t cap,
+                        uint64_t *n);
+
+/* Run a model on host feature rows: y (n floats).  tensor_cores = 1 uses the
+ * kernel of the learned mode (BF16 tcgen05), 0 an FP32 CUDA-core kernel. */
+int gls_presize_predict(gls_ctx *ctx, const gls_presize_model *model, const float *feat, uint64_t n,
+                        float *y, int tensor_cores);
+
+/* Training on the GPU (FP32, Adam, Huber loss on y - log(1 + count)). */
+typedef struct gls_trainer gls_trainer;
+typedef struct {
+    uint32_t batch;        /* rows per step */
+    uint32_t epochs;
+    float lr;              /* Adam step size */
+    float huber;           /* Huber threshold on the log-length error */
+    uint64_t seed;         /* shuffling and initialization */
+} gls_train_opts;
+
+int gls_trainer_create(int device, uint64_t seed, gls_trainer **out);
+int gls_trainer_destroy(gls_trainer *tr);
+const char *gls_trainer_error(const gls_trainer *tr);
+/* Copy n training rows (feat n x 32, target n = log(1 + count)) to the device. */
+int gls_trainer_set_data(gls_trainer *tr, const float *feat, const float *target, uint64_t n);
+/* Train; loss receives the mean loss of every epoch (opts->epochs floats). */
+int gls_trainer_fit(gls_trainer *tr, const gls_train_opts *opts, float *loss);
+/* Loss and gradient of every parameter (GLS_MLP_PARAMS floats) over rows
+ * [first, first + n) of the data, without updating (for gradient checks). */
+int gls_trainer_grad(gls_trainer *tr, uint64_t first, uint64_t n, float huber, float *grad, float *loss);
+int gls_trainer_get_params(gls_trainer *tr, float *params);
+int gls_trainer_set_params(gls_trainer *tr, const float *params);
 
 /* Simulate gate outputs [first, first + count) of one level (in the
  * library's order inside the level; count up to the level's number of gate
