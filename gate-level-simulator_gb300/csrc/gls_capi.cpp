@@ -62,7 +62,6 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
     a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
-    a->pred = ctx->pred.as<uint32_t>();
 }
 
 namespace {
@@ -143,6 +142,7 @@ static void free_window(Window *w)
     w->pool.release(); w->net_off.release(); w->net_len.release();
     w->init_off.release(); w->init_len.release(); w->saif.release(); w->small.release();
     w->stim_dev.release();
+    w->dwin.release();
     w->h_words.release(); w->h_off.release(); w->h_len.release();
     delete w;
 }
@@ -160,6 +160,19 @@ extern "C" int gls_clear_windows(gls_ctx *ctx)
     return GLS_OK;
 }
 
+void ctx_drop_graphs(gls_ctx *ctx)
+{
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+    ctx->graphs.clear();
+}
+
+// a window's large device buffers go; its SAIF counts, lengths and flags stay
+static void release_window_pool(Window *w)
+{
+    w->pool.release(); w->net_off.release(); w->init_off.release(); w->init_len.release(); w->stim_dev.release();
+    w->uploaded = false;
+}
+
 extern "C" int gls_destroy(gls_ctx *ctx)
 {
     if (!ctx) return GLS_EINVAL;
@@ -167,9 +180,15 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     for (Window *w : ctx->spare) free_window(w);
     ctx->spare.clear();
     ctx->meta.release(); ctx->arcs.release(); ctx->ndel.release(); ctx->lut.release();
-    ctx->copies.release();
-    ctx->seg_base.release(); ctx->slot.release(); ctx->scr.release(); ctx->segs.release();
-    ctx->scratch.release();
+    ctx_drop_graphs(ctx);
+    ctx->hwave.release();
+    ctx->dwave.release();
+    for (LevelScratch *l : ctx->lsc) {
+        l->release();
+        delete l;
+    }
+    ctx->lsc.clear();
+    ctx->feat_static.release(); ctx->mlp_params.release(); ctx->mlp_img.release(); ctx->aux.release();
     for (cudaEvent_t e : ctx->prof) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -399,14 +418,11 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     CK(cudaMemcpy(ctx->ndel.p, h_ndel.data(), h_ndel.size() * sizeof(NetDelay), cudaMemcpyHostToDevice),
        "upload net delays");
     CK(cudaMemcpy(ctx->lut.p, h_lut.data(), h_lut.size(), cudaMemcpyHostToDevice), "upload lut");
-    CK(ctx->seg_base.ensure((size_t)(ctx->max_width + 1) * 4), "alloc seg_base");
-    CK(ctx->slot.ensure((size_t)(ctx->max_width + 1) * 8), "alloc slot");
-    CK(ctx->scr.ensure((size_t)(ctx->max_width + 1) * 8), "alloc scratch offsets");
-    CK(ctx->res.ensure((size_t)(ctx->max_width + 1) * 4), "alloc reserved lengths");
-    CK(ctx->pred.ensure((size_t)(ctx->max_width + 1) * 4), "alloc presize predictions");
+    ctx_drop_graphs(ctx);   // they hold the previous netlist's tables
     ctx->seg_cap = std::max<uint32_t>(1u << 21, 8 * ctx->max_width + 64);
-    CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "alloc segs");
-    CK(ctx->copies.ensure((size_t)ctx->seg_cap * sizeof(CopyRec)), "alloc copies");
+    if (ctx->lsc.empty()) ctx->lsc.push_back(new LevelScratch);
+    for (LevelScratch *l : ctx->lsc) l->release();
+    CK(ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work space");
     ctx->loaded = true;
     return GLS_OK;
 }
@@ -441,6 +457,7 @@ static int upload_window(gls_ctx *ctx, Window *w)
                            ctx->stream),
            "upload stim nets");
     CK(cudaStreamSynchronize(ctx->stream), "upload sync");
+    w->uploaded = true;
     return GLS_OK;
 }
 
@@ -543,20 +560,22 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
         uint64_t want = (uint64_t)(2.0 * avg * 6.0 * ctx->max_width) + 16ull * ctx->max_width + 4096;
         if (want > ctx->scr_cap) {
-            CK(ctx->scratch.ensure(want * 4), "alloc level scratch");
             ctx->scr_cap = want;
+            CK(ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level scratch");
         }
     }
-    int rc = upload_window(ctx, w);
-    if (rc) { free_window(w); return rc; }
+    // device buffers are filled when the window first runs
+    w->uploaded = false;
+    w->saif_only = false;
     ctx->windows.push_back(w);
     if (window_id) *window_id = (uint32_t)(ctx->windows.size() - 1);
     return GLS_OK;
 }
 
-static WinDev make_windev(gls_ctx *ctx, Window *w)
+static WinDev make_windev(gls_ctx *ctx, Window *w, const LevelScratch &ls)
 {
     WinDev d;
+    std::memset(&d, 0, sizeof d);
     d.net_off = w->net_off.as<uint64_t>();
     d.net_len = w->net_len.as<uint32_t>();
     d.pool = w->pool.as<uint32_t>();
@@ -567,16 +586,19 @@ static WinDev make_windev(gls_ctx *ctx, Window *w)
     d.err = reinterpret_cast<uint32_t *>(sm + 5);
     d.n_segs = reinterpret_cast<uint32_t *>(sm + 6);
     d.n_over = sm + 7;
-    d.res = ctx->res.as<uint32_t>();
-    d.seg_base = ctx->seg_base.as<uint32_t>();
-    d.slot = ctx->slot.as<uint64_t>();
-    d.scr = ctx->scr.as<uint64_t>();
-    d.segs = ctx->segs.as<SegRec>();
-    d.copies = ctx->copies.as<CopyRec>();
-    d.scratch = ctx->scratch.as<uint32_t>();
-    d.scr_cap = ctx->scr_cap;
+    d.res = ls.res.as<uint32_t>();
+    d.pred = ls.pred.as<uint32_t>();
+    d.stim_nets = w->stim_dev.as<uint32_t>();
+    d.n_stim = (uint32_t)w->stim_nets.size();
+    d.seg_base = ls.seg_base.as<uint32_t>();
+    d.slot = ls.slot.as<uint64_t>();
+    d.scr = ls.scr.as<uint64_t>();
+    d.segs = ls.segs.as<SegRec>();
+    d.copies = ls.copies.as<CopyRec>();
+    d.scratch = ls.scratch.as<uint32_t>();
+    d.scr_cap = ls.scr_cap;
     d.cap = w->cap;
-    d.seg_cap = ctx->seg_cap;
+    d.seg_cap = ls.seg_cap;
     d.t_begin = w->t_begin;
     d.t_end = w->t_end;
     return d;
@@ -600,7 +622,8 @@ static void prof_mark(gls_ctx *ctx)
     if (e) cudaEventRecord(e, ctx->stream);
 }
 
-static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
+// Clear a window's outputs and counters before it runs.
+static int reset_window(gls_ctx *ctx, Window *w)
 {
     const uint64_t n = ctx->n_nets;
     CK(cudaMemcpyAsync(w->net_off.p, w->init_off.p, n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "reset offsets");
@@ -608,11 +631,20 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     CK(cudaMemsetAsync(w->saif.p, 0xFF, n * 24, ctx->stream), "reset saif");
     unsigned long long small[8] = {w->stim_events + ctx->pool_gap, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(w->small.p, small, sizeof small, cudaMemcpyHostToDevice, ctx->stream), "reset counters");
-    WinDev d = make_windev(ctx, w);
-    prof_mark(ctx);
-    launch_stim_saif(d, w->stim_dev.as<uint32_t>(), (uint32_t)w->stim_nets.size(), ctx->stream);
+    return GLS_OK;
+}
+
+// The launches of a run of nwin windows (device array dw): stimulus SAIF,
+// then per level the presize (learned mode), plan, simulate per fan-in
+// class, link and copy.  With `prof` the kernel classes are bracketed with
+// events (not during stream capture).
+static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint32_t nwin, uint32_t max_stim,
+                          bool prof, uint32_t *launches)
+{
+    if (prof) prof_mark(ctx);
+    launch_stim_saif(dw, h0, nwin, max_stim, ctx->stream);
     ++*launches;
-    prof_mark(ctx);
+    if (prof) prof_mark(ctx);
     LevelArgs a;
     ctx_level_args(ctx, &a);
     for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
@@ -623,32 +655,123 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
             // the level's presize predictions (tensor cores) before its slots are planned
             PresizeArgs pa;
             ctx_presize_args(ctx, &pa);
-            pa.net_len = d.net_len;
-            pa.saif = d.saif;
+            pa.wv = dw;
+            pa.nwin = nwin;
             pa.lo = a.lo;
             pa.n = a.hi - a.lo;
-            pa.pred = ctx->pred.as<uint32_t>();
-            pa.err = d.err;
             launch_presize(pa, true, ctx->stream);
             ++*launches;
         }
-        launch_plan(d, a, ctx->stream);
-        prof_mark(ctx);
+        launch_plan(dw, h0, nwin, a, ctx->stream);
+        if (prof) prof_mark(ctx);
         for (int c = 0; c < kClasses; ++c) {
             const uint32_t d0 = ctx->cls_start[(kClasses + 1) * L + c], d1 = ctx->cls_start[(kClasses + 1) * L + c + 1];
             if (d1 > d0) {
-                launch_sim(d, a, c, d0, d1, ctx->sm_count, ctx->stream);
+                launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, ctx->stream);
                 ++*launches;
             }
         }
-        prof_mark(ctx);
-        launch_link(d, a, ctx->stream);
-        launch_copy(d, a, ctx->sm_count, ctx->stream);
-        prof_mark(ctx);
+        if (prof) prof_mark(ctx);
+        launch_link(dw, h0, nwin, a, ctx->stream);
+        launch_copy(dw, h0, nwin, a, ctx->sm_count, ctx->stream);
+        if (prof) prof_mark(ctx);
         *launches += 3;
     }
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;
+}
+
+static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
+{
+    int rc = w->uploaded ? GLS_OK : upload_window(ctx, w);
+    if (rc) return rc;
+    w->saif_only = false;
+    rc = reset_window(ctx, w);
+    if (rc) return rc;
+    const WinDev d = make_windev(ctx, w, *ctx->lsc[0]);
+    CK(w->dwin.ensure(sizeof(WinDev)), "alloc window descriptor");
+    CK(cudaMemcpyAsync(w->dwin.p, &d, sizeof d, cudaMemcpyHostToDevice, ctx->stream), "upload window descriptor");
+    return enqueue_levels(ctx, w->dwin.as<WinDev>(), d, 1, d.n_stim, true, launches);
+}
+
+// Totals of a run over its windows.
+struct RunAcc {
+    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0, over_ev = 0;
+    double total_ms = 0.0;
+    uint32_t launches = 0;
+};
+
+// Read a window's flags after its run; on a full pool or work space, grow it
+// and run the window again on its own (level work space 0), until it fits.
+static int settle_window(gls_ctx *ctx, Window *w, RunAcc &acc)
+{
+    for (int attempt = 0;; ++attempt) {
+        unsigned long long small[8];
+        CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
+        const uint32_t err = (uint32_t)small[5];
+        if (!err) {
+            acc.over_ev += small[7];
+            acc.gate_ev += small[1];
+            acc.out_ev += small[2];
+            acc.segs += small[3];
+            acc.fanin_ev += small[4];
+            acc.pool_ev += small[0];
+            acc.pool_bytes += w->cap * 4;
+            break;
+        }
+        if (err & kErrPresize) return fail(ctx, GLS_ECUDA, "presize kernel timed out waiting for its tensor-core MMA");
+        if (err & (kErrRegion | kErrEmptied | kErrTime)) {
+            return fail(ctx, err & kErrTime ? GLS_ERANGE : GLS_EINVAL,
+                        "simulation error flags 0x%x (%s)", err,
+                        err & kErrTime ? "output time reached 2^32-1"
+                                       : err & kErrEmptied ? "output list emptied by a zero delay at time 0"
+                                                           : "segment region overflow");
+        }
+        if (attempt > 12) return fail(ctx, GLS_EOVERFLOW, "event pool could not grow enough");
+        if (err & kErrSegCap) ctx->seg_cap = std::max<uint32_t>(ctx->seg_cap, ctx->lsc[0]->seg_cap) * 2;
+        if (err & kErrScratch) ctx->scr_cap = std::max<uint64_t>(ctx->scr_cap, ctx->lsc[0]->scr_cap) * 2;
+        CK(ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "grow level work space");
+        if (err & kErrPool) {
+            w->cap *= 2;
+            w->pool.release();
+            int rc = upload_window(ctx, w);
+            if (rc) return fail(ctx, GLS_EOVERFLOW, "event pool growth to %llu events failed: %s",
+                                (unsigned long long)w->cap, ctx->err.c_str());
+            ctx->stats.overflow_retries++;
+        }
+        uint32_t l2 = 0;
+        ctx->prof_used = 0;   // per-kernel times then cover the successful run only
+        CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+        int rc = enqueue_window(ctx, w, &l2);
+        if (rc) return rc;
+        CK(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+        CK(cudaStreamSynchronize(ctx->stream), "rerun");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        acc.total_ms += ms;
+        acc.launches += l2;
+    }
+    w->done = true;
+    return GLS_OK;
+}
+
+static void publish_stats(gls_ctx *ctx, const RunAcc &acc, const double kms[4])
+{
+    ctx->stats.gate_events = acc.gate_ev;
+    ctx->stats.output_events = acc.out_ev;
+    ctx->stats.segments = acc.segs;
+    ctx->stats.pool_events = acc.pool_ev;
+    ctx->stats.pool_bytes = acc.pool_bytes;
+    ctx->stats.kernel_ms = acc.total_ms;
+    ctx->stats.launches = acc.launches;
+    ctx->stats.n_windows = (uint32_t)ctx->windows.size();
+    ctx->stats.stim_ms = kms[0];
+    ctx->stats.plan_ms = kms[1];
+    ctx->stats.sim_ms = kms[2];
+    ctx->stats.combine_ms = kms[3];
+    ctx->stats.fanin_bytes = acc.fanin_ev * 5;
+    ctx->stats.presize_overflows = acc.over_ev;
+    ctx->stats.pool_used = acc.pool_ev;
 }
 
 extern "C" int gls_run(gls_ctx *ctx)
@@ -692,77 +815,127 @@ extern "C" int gls_run(gls_ctx *ctx)
             }
         }
     }
-    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0, over_ev = 0;
-    // check every window; regrow the pool or the segment table and rerun
+    RunAcc acc;
+    acc.total_ms = total_ms;
+    acc.launches = launches;
     for (Window *w : ctx->windows) {
-        for (int attempt = 0;; ++attempt) {
-            unsigned long long small[8];
-            CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
-            const uint32_t err = (uint32_t)small[5];
-            if (!err) {
-                over_ev += small[7];
-                gate_ev += small[1];
-                out_ev += small[2];
-                segs += small[3];
-                fanin_ev += small[4];
-                pool_ev += small[0];
-                pool_bytes += w->cap * 4;
-                break;
-            }
-            if (err & kErrPresize) return fail(ctx, GLS_ECUDA, "presize kernel timed out waiting for its tensor-core MMA");
-            if (err & (kErrRegion | kErrEmptied | kErrTime)) {
-                return fail(ctx, err & kErrTime ? GLS_ERANGE : GLS_EINVAL,
-                            "simulation error flags 0x%x (%s)", err,
-                            err & kErrTime ? "output time reached 2^32-1"
-                                           : err & kErrEmptied ? "output list emptied by a zero delay at time 0"
-                                                               : "segment region overflow");
-            }
-            if (attempt > 12) return fail(ctx, GLS_EOVERFLOW, "event pool could not grow enough");
-            if (err & kErrSegCap) {
-                ctx->seg_cap *= 2;
-                CK(ctx->segs.ensure((size_t)ctx->seg_cap * sizeof(SegRec)), "grow segs");
-                CK(ctx->copies.ensure((size_t)ctx->seg_cap * sizeof(CopyRec)), "grow copies");
-            }
-            if (err & kErrScratch) {
-                ctx->scr_cap *= 2;
-                CK(ctx->scratch.ensure(ctx->scr_cap * 4), "grow level scratch");
-            }
-            if (err & kErrPool) {
-                w->cap *= 2;
-                w->pool.release();
-                int rc = upload_window(ctx, w);
-                if (rc) return fail(ctx, GLS_EOVERFLOW, "event pool growth to %llu events failed: %s",
-                                    (unsigned long long)w->cap, ctx->err.c_str());
-                ctx->stats.overflow_retries++;
-            }
-            uint32_t l2 = 0;
-            ctx->prof_used = 0;   // per-kernel times then cover the successful run only
-            CK(cudaEventRecord(ctx->ev0, ctx->stream), "event");
-            int rc = enqueue_window(ctx, w, &l2);
-            if (rc) return rc;
-            CK(cudaEventRecord(ctx->ev1, ctx->stream), "event");
-            CK(cudaStreamSynchronize(ctx->stream), "rerun");
-            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-            total_ms += ms;
-            launches += l2;
-        }
-        w->done = true;
+        int rc = settle_window(ctx, w, acc);
+        if (rc) return rc;
     }
-    ctx->stats.gate_events = gate_ev;
-    ctx->stats.output_events = out_ev;
-    ctx->stats.segments = segs;
-    ctx->stats.pool_events = pool_ev;
-    ctx->stats.pool_bytes = pool_bytes;
-    ctx->stats.kernel_ms = total_ms;
-    ctx->stats.launches = launches;
-    ctx->stats.n_windows = (uint32_t)ctx->windows.size();
-    ctx->stats.stim_ms = kms[0];
-    ctx->stats.plan_ms = kms[1];
-    ctx->stats.sim_ms = kms[2];
-    ctx->stats.combine_ms = kms[3];
-    ctx->stats.fanin_bytes = fanin_ev * 5;
-    ctx->stats.presize_overflows = over_ev;
-    ctx->stats.pool_used = pool_ev;
+    publish_stats(ctx, acc, kms);
+    return GLS_OK;
+}
+
+extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
+{
+    if (!ctx) return GLS_EINVAL;
+    if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "run before load_netlist");
+    if (ctx->opts.alloc_mode == GLS_ALLOC_LEARNED && !ctx->have_model)
+        return fail(ctx, GLS_ESTATE, "GLS_ALLOC_LEARNED needs gls_set_presize_model before gls_run_batched");
+    gls_batch_opts o{0, 1, 0};
+    if (opts) o = *opts;
+    cudaSetDevice(ctx->opts.device);
+    const size_t nw = ctx->windows.size();
+    RunAcc acc;
+    const double kms[4] = {0, 0, 0, 0};
+    if (!nw) {
+        publish_stats(ctx, acc, kms);
+        return GLS_OK;
+    }
+    if (o.saif_only)
+        for (Window *w : ctx->windows) release_window_pool(w);
+    // windows per wave: all of them, or with saif_only as many as free device
+    // memory holds (each needs its pool, net tables and a level work space)
+    uint64_t B = std::min<uint64_t>(nw, kMaxWave);
+    if (o.max_wave) B = std::min<uint64_t>(B, o.max_wave);
+    if (o.saif_only) {
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        uint64_t per = 0;
+        for (Window *w : ctx->windows) per = std::max<uint64_t>(per, w->cap * 4);
+        per += (uint64_t)ctx->n_nets * 48 + (uint64_t)(ctx->max_width + 1) * 32 +
+               (uint64_t)ctx->seg_cap * (sizeof(SegRec) + sizeof(CopyRec)) + ctx->scr_cap * 4;
+        const uint64_t fit = std::max<uint64_t>(1, (uint64_t)(0.85 * (double)fr) / std::max<uint64_t>(per, 1));
+        B = std::max<uint64_t>(1, std::min(B, fit));
+    }
+    while (ctx->lsc.size() < B) ctx->lsc.push_back(new LevelScratch);
+    for (uint64_t k = 0; k < B; ++k)
+        CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
+    if (!ctx->hwave.ensure(kMaxWave * sizeof(WinDev))) return fail(ctx, GLS_ENOMEM, "pinned wave descriptors");
+    CK(ctx->dwave.ensure(kMaxWave * sizeof(WinDev)), "alloc wave descriptors");
+    WinDev *hw = ctx->hwave.as<WinDev>();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    float run_ms = 0.f;
+    int rc = GLS_OK;
+    for (size_t w0 = 0; w0 < nw && rc == GLS_OK; w0 += B) {
+        const uint32_t nwin = (uint32_t)std::min<uint64_t>(B, nw - w0);
+        uint32_t max_stim = 0;
+        for (uint32_t k = 0; k < nwin && rc == GLS_OK; ++k) {
+            Window *w = ctx->windows[w0 + k];
+            if (!w->uploaded) rc = upload_window(ctx, w);
+            if (rc == GLS_OK) rc = reset_window(ctx, w);
+            w->saif_only = false;
+            hw[k] = make_windev(ctx, w, *ctx->lsc[k]);
+            max_stim = std::max(max_stim, hw[k].n_stim);
+        }
+        if (rc) break;
+        cudaEventRecord(e0, ctx->stream);
+        cudaError_t e = cudaMemcpyAsync(ctx->dwave.p, hw, nwin * sizeof(WinDev), cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "upload wave descriptors: %s", cudaGetErrorString(e)); break; }
+        const WinDev *dw = ctx->dwave.as<WinDev>();
+        if (o.use_graph && nwin > 1) {
+            // one graph per wave shape; the descriptors it reads are rewritten per wave
+            const uint64_t key = (uint64_t)nwin | ((uint64_t)max_stim << 11) | ((uint64_t)ctx->warp_mask << 43) |
+                                 ((uint64_t)ctx->opts.alloc_mode << 46);
+            cudaGraphExec_t ge = nullptr;
+            uint32_t l = 0;
+            for (auto &g : ctx->graphs)
+                if (g.key == key) {
+                    ge = g.exec;
+                    l = g.launches;
+                }
+            if (!ge) {
+                cudaGraph_t g = nullptr;
+                e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &l);
+                    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+                    if (rc == GLS_OK && e2 != cudaSuccess) e = e2;
+                }
+                if (rc == GLS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (rc) break;
+                if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "capture wave graph: %s", cudaGetErrorString(e)); break; }
+                ctx->graphs.push_back({key, ge, l});
+            }
+            e = cudaGraphLaunch(ge, ctx->stream);
+            if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "graph launch: %s", cudaGetErrorString(e)); break; }
+            acc.launches += l;
+        } else {
+            rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &acc.launches);
+            if (rc) break;
+        }
+        cudaEventRecord(e1, ctx->stream);
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "wave: %s", cudaGetErrorString(e)); break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        run_ms += ms;
+        for (uint32_t k = 0; k < nwin && rc == GLS_OK; ++k) rc = settle_window(ctx, ctx->windows[w0 + k], acc);
+        if (o.saif_only)
+            for (uint32_t k = 0; k < nwin; ++k) {
+                Window *w = ctx->windows[w0 + k];
+                release_window_pool(w);
+                w->saif_only = true;
+            }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    acc.total_ms += run_ms;
+    publish_stats(ctx, acc, kms);
     return GLS_OK;
 }
 
@@ -806,6 +979,7 @@ extern "C" int gls_waveform(gls_ctx *ctx, uint32_t window, uint32_t net, uint32_
     Window *w = get_done(ctx, window);
     if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
     if (net >= ctx->n_nets) return fail(ctx, GLS_EINVAL, "net %u out of range", net);
+    if (w->saif_only) return fail(ctx, GLS_ESTATE, "window %u ran with saif_only: its waveforms were not kept", window);
     cudaSetDevice(ctx->opts.device);
     uint64_t off = 0;
     uint32_t len = 0;

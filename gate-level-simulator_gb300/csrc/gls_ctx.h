@@ -53,6 +53,47 @@ struct PinBuf {   // page-locked host staging, reused across windows
     template <typename T> T *as() const { return static_cast<T *>(p); }
 };
 
+// One window's per-level work space: segment tables, slot offsets and the
+// segment stacks.  Sequential runs share set 0; a wave of windows run
+// together takes one set per window.
+struct LevelScratch {
+    DevBuf seg_base, slot, scr, res, pred, segs, copies, scratch;
+    uint32_t seg_cap = 0;
+    uint64_t scr_cap = 0;
+    uint32_t width = 0;
+    cudaError_t ensure(uint32_t w, uint32_t segs_need, uint64_t words_need)
+    {
+        cudaError_t e = cudaSuccess;
+        if (w > width) {
+            const size_t n = (size_t)w + 1;
+            if (e == cudaSuccess) e = seg_base.ensure(n * 4);
+            if (e == cudaSuccess) e = slot.ensure(n * 8);
+            if (e == cudaSuccess) e = scr.ensure(n * 8);
+            if (e == cudaSuccess) e = res.ensure(n * 4);
+            if (e == cudaSuccess) e = pred.ensure(n * 4);
+            if (e == cudaSuccess) width = w;
+        }
+        if (e == cudaSuccess && segs_need > seg_cap) {
+            e = segs.ensure((size_t)segs_need * sizeof(gls::SegRec));
+            if (e == cudaSuccess) e = copies.ensure((size_t)segs_need * sizeof(gls::CopyRec));
+            if (e == cudaSuccess) seg_cap = segs_need;
+        }
+        if (e == cudaSuccess && words_need > scr_cap) {
+            e = scratch.ensure(words_need * 4);
+            if (e == cudaSuccess) scr_cap = words_need;
+        }
+        return e;
+    }
+    void release()
+    {
+        DevBuf *all[] = {&seg_base, &slot, &scr, &res, &pred, &segs, &copies, &scratch};
+        for (DevBuf *b : all) b->release();
+        seg_cap = 0;
+        scr_cap = 0;
+        width = 0;
+    }
+};
+
 struct Window {
     std::vector<uint32_t> stim_nets;
     std::vector<uint64_t> stim_off;     // aligned pool offset per stimulus net
@@ -63,7 +104,10 @@ struct Window {
     uint64_t t_begin = 0, t_end = 0;
     uint64_t cap = 0;
     DevBuf pool, net_off, net_len, init_off, init_len, saif, small, stim_dev;
+    DevBuf dwin;                        // the window's WinDev on the device (sequential runs)
     bool done = false;
+    bool uploaded = false;              // device buffers hold this stimulus (uploaded when the window first runs)
+    bool saif_only = false;             // pool released after a batched run: SAIF counts and lengths kept
 };
 
 }  // namespace glsh
@@ -85,16 +129,15 @@ struct gls_ctx {
     std::vector<uint8_t> driven;             // net driven by a gate output
     std::vector<uint32_t> ext_inputs;        // nets read by gates and driven by no gate
     DevBuf meta, arcs, ndel, lut;
-    DevBuf seg_base, slot, scr, segs, copies, scratch;
-    uint32_t seg_cap = 0;
-    uint64_t scr_cap = 0;
+    std::vector<LevelScratch *> lsc;         // level work spaces ([0]: sequential runs)
+    uint32_t seg_cap = 0;                    // segment-table size new work spaces get
+    uint64_t scr_cap = 0;                    // stack words new work spaces get
     uint32_t def_delay = 1;
     uint32_t warp_mask = 0;          // fan-in classes run by the warp-per-segment kernel (GLS_SIM_WARP_MASK)
     uint32_t seg_target_w = 0;       // segments per class for those kernels (GLS_SIM_WARP_SEGS per SM)
     uint64_t pool_gap = 0;           // unused events between the stimulus and the first gate output (GLS_POOL_GAP_EVENTS)
     // learned presize (GLS_ALLOC_LEARNED)
     DevBuf feat_static;              // per driver x 32 static features
-    DevBuf pred, res;                // per driver of the widest level: predicted / reserved events
     DevBuf mlp_params, mlp_img;      // FP32 parameters and the BF16 weight image
     DevBuf aux;                      // small device scratch of the presize calls (error word)
     bool have_model = false;
@@ -106,6 +149,16 @@ struct gls_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<cudaEvent_t> prof;   // per-launch events when opts.profile
     size_t prof_used = 0;
+    // batched runs: the wave's window descriptors (host pinned, device) and
+    // the captured launch graphs, one per wave shape
+    PinBuf hwave;
+    DevBuf dwave;
+    struct WaveGraph {
+        uint64_t key;
+        cudaGraphExec_t exec;
+        uint32_t launches;
+    };
+    std::vector<WaveGraph> graphs;
 };
 
 
@@ -116,3 +169,5 @@ void ctx_level_args(const gls_ctx *ctx, gls::LevelArgs *a);
 namespace gls { struct PresizeArgs; }
 // The presize-kernel arguments of the installed model (rows, range and outputs left empty).
 void ctx_presize_args(const gls_ctx *ctx, gls::PresizeArgs *a);
+// Forget the captured wave graphs (they bake in tables and options).
+void ctx_drop_graphs(gls_ctx *ctx);

@@ -127,12 +127,16 @@ struct WinDev {
     uint32_t *n_segs;
     uint32_t *res;              // per driver of the level: events reserved in its slot (exact / learned modes)
     unsigned long long *n_over; // gate outputs placed exactly because the presize was short (learned mode)
+    uint32_t *pred;             // per driver of the level: predicted slot length (learned mode)
+    const uint32_t *stim_nets;  // nets the stimulus drives
     uint32_t *scratch;          // level scratch: segment stacks (event words)
     uint64_t cap;               // pool capacity (events)
     uint64_t scr_cap;           // scratch capacity (events)
-    uint32_t seg_cap;           // SegRec capacity
     uint64_t t_begin, t_end;
+    uint32_t seg_cap;           // SegRec capacity
+    uint32_t n_stim;
 };
+static_assert(sizeof(WinDev) <= 192, "WinDev fits the static entry point's descriptor slot");
 
 struct LevelArgs {
     const DrvMeta *meta;
@@ -146,17 +150,22 @@ struct LevelArgs {
     uint32_t warp_mask;         // bit c: fan-in class c runs the warp-per-segment kernel
     uint32_t def_delay;         // delay used when no arc applies
     uint32_t alloc_mode;        // kAllocBound / kAllocExact / kAllocLearned
-    const uint32_t *pred;       // learned mode: predicted slot length per driver of the level
 };
+
+// Windows simulated together: every level kernel takes a device array of
+// WinDev and covers all of them in one launch (at most kMaxWave).
+constexpr uint32_t kMaxWave = 1024;
 
 // fan-in class of a gate output by its number of distinct input nets
 __host__ __device__ inline int fanin_class(int m) { return m <= 1 ? 0 : (m == 2 ? 1 : (m == 3 ? 2 : 3)); }
 
-void launch_stim_saif(const WinDev &w, const uint32_t *stim_nets, uint32_t n_stim, cudaStream_t st);
-void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st);
-void launch_sim(const WinDev &w, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
-                cudaStream_t st);
-void launch_link(const WinDev &w, const LevelArgs &a, cudaStream_t st);
-void launch_copy(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st);
+// A launch covers nwin windows: `h` is window 0's descriptor on the host
+// (used when nwin == 1), `dw` the device array of all nwin descriptors.
+void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, cudaStream_t st);
+void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
+void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,
+                int sm_count, cudaStream_t st);
+void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
+void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st);
 
 }  // namespace gls

@@ -27,6 +27,7 @@
 // entry is dropped iff it repeats the value of the last kept entry before it.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 #include "gls_internal.h"
 
 namespace gls {
@@ -151,14 +152,36 @@ __device__ T block_excl_scan(T x, T *total, T *sm)
     return pre + inc - x;
 }
 
-__global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
+// The windows a launch covers: one window passed by value (kernel
+// parameter space, no indirection in the hot loops), or a device array.
+template <bool kBatch> struct WinSet;
+template <> struct WinSet<false> {
+    WinDev w;
+    __device__ __forceinline__ const WinDev &get(uint32_t) const { return w; }
+    __device__ __forceinline__ uint32_t size() const { return 1; }
+};
+template <> struct WinSet<true> {
+    const WinDev *wv;
+    uint32_t n;
+    __device__ __forceinline__ const WinDev &get(uint32_t k) const { return wv[k]; }
+    __device__ __forceinline__ uint32_t size() const { return n; }
+};
+
+// one block per window
+template <bool kBatch>
+__global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArgs a)
 {
     __shared__ unsigned long long sm64[32];
     __shared__ uint32_t sm32[32];
     __shared__ uint32_t s_seg[kClasses];
     __shared__ unsigned long long s_base;
-    if (*w.err) return;
+    const WinDev &w = ws.get(blockIdx.x);
     const uint32_t n = a.hi - a.lo;
+    if (*w.err) {   // a failed window: an empty segment table keeps the later kernels off it
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) w.seg_base[i] = 0;
+        if (threadIdx.x == 0) *w.n_segs = 0;
+        return;
+    }
     // fan-in events of the level per fan-in class: every class runs as its
     // own launch, so every class is split into about seg_target segments
     unsigned long long e_cls[kClasses] = {0, 0, 0, 0}, g_tot = 0;
@@ -202,7 +225,11 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
         atomicAdd(&w.counters[3], e_tot);
     }
     __syncthreads();
-    if (*w.err) return;
+    if (*w.err) {
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) w.seg_base[i] = 0;
+        if (threadIdx.x == 0) *w.n_segs = 0;
+        return;
+    }
     const unsigned long long base = s_base;
     uint32_t run_seg = 0;
     unsigned long long run_slot = 0, run_scr = 0;
@@ -218,7 +245,7 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
             slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
             if (a.alloc_mode == kAllocExact) slot = 0;
-            else if (a.alloc_mode == kAllocLearned) slot = min(slot, ((unsigned long long)a.pred[i] + 3) & ~3ull);
+            else if (a.alloc_mode == kAllocLearned) slot = min(slot, ((unsigned long long)w.pred[i] + 3) & ~3ull);
             if (a.alloc_mode != kAllocBound) w.res[i] = (uint32_t)slot;
             scr = (E + S + 3) & ~3ull;      // segment stacks: events of the segment (+1 for the first)
         }
@@ -238,14 +265,23 @@ __global__ void __launch_bounds__(1024) k_plan(WinDev w, LevelArgs a)
         run_slot += tSlot;
         run_scr += tScr;
     }
+    __shared__ bool s_fail;
     if (threadIdx.x == 0) {
         w.seg_base[n] = run_seg;
         *w.n_segs = run_seg;
-        if (run_seg > w.seg_cap) atomicOr(w.err, kErrSegCap);
-        if (run_scr > w.scr_cap) atomicOr(w.err, kErrScratch);
-        if (base + run_slot > w.cap) atomicOr(w.err, kErrPool);
+        uint32_t e = 0;
+        if (run_seg > w.seg_cap) e |= kErrSegCap;
+        if (run_scr > w.scr_cap) e |= kErrScratch;
+        if (base + run_slot > w.cap) e |= kErrPool;
         else *w.top = base + run_slot;
+        if (e) atomicOr(w.err, e);
+        s_fail = e != 0;
         atomicAdd(&w.counters[2], (unsigned long long)run_seg);
+    }
+    __syncthreads();
+    if (s_fail) {
+        for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) w.seg_base[i] = 0;
+        if (threadIdx.x == 0) *w.n_segs = 0;
     }
 }
 
@@ -432,25 +468,81 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     w.segs[seg_id] = r;
 }
 
+// Segments of all windows of a launch form one index space: s_pre[k] is
+// the first index of window k.
+// skip_err leaves out windows whose error flag is set; only kernels during
+// which no flag can change may use it (all blocks must see the same counts).
+template <bool kSkipErr, bool kBatch, class Count>
+__device__ uint32_t window_prefix(const WinSet<kBatch> &ws, Count count, uint32_t *s_pre, uint32_t *sm32)
+{
+    const uint32_t nwin = ws.size();
+    if (!kBatch) {   // one window: no scan
+        const WinDev &w = ws.get(0);
+        const uint32_t v = (kSkipErr && *w.err) ? 0u : count(w);
+        if (threadIdx.x == 0) { s_pre[0] = 0; s_pre[1] = v; }
+        __syncthreads();
+        return v;
+    }
+    uint32_t run = 0;
+    for (uint32_t c = 0; c < nwin; c += blockDim.x) {
+        const uint32_t k = c + threadIdx.x;
+        uint32_t v = 0;
+        if (k < nwin && !(kSkipErr && *ws.get(k).err)) v = count(ws.get(k));
+        uint32_t tot;
+        const uint32_t x = block_excl_scan<uint32_t>(v, &tot, sm32);
+        if (k < nwin) s_pre[k] = run + x;
+        run += tot;
+    }
+    if (threadIdx.x == 0) s_pre[nwin] = run;
+    __syncthreads();
+    return run;
+}
+
+// the window holding index q: the last k with s_pre[k] <= q
+__device__ __forceinline__ uint32_t window_of(const uint32_t *s_pre, uint32_t nwin, uint32_t q)
+{
+    if (nwin == 1) return 0;
+    uint32_t lo = 0, hi = nwin;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_pre[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 // Gates of a level are sorted by fan-in class; one instantiation per class
 // keeps the register budget of the common narrow gates small.  Each block
 // owns a contiguous share of the class's segments and its threads take the
 // next one from a shared counter as they finish, so long and short segments
 // balance inside the block.
-template <int M>
-__global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4)) k_sim(WinDev w, LevelArgs a, uint32_t d0, uint32_t d1)
+template <int M, bool kBatch>
+__global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4))
+    k_sim(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     __shared__ uint32_t s_next;
-    if (*w.err) return;
-    const uint32_t g0 = w.seg_base[d0], g1 = w.seg_base[d1];
-    const uint32_t total = g1 - g0;
+    __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
+    __shared__ uint32_t sm32[32];
+    const uint32_t nwin = ws.size();
+    // segment indices: the window's own for one window, else one space over
+    // all windows (a window whose plan failed has an all-zero segment table)
+    uint32_t g0 = 0, total;
+    if (kBatch) {
+        total = window_prefix<false>(
+            ws, [&](const WinDev &x) { return x.seg_base[d1] - x.seg_base[d0]; }, s_pre, sm32);
+    } else {
+        g0 = ws.get(0).seg_base[d0];
+        total = ws.get(0).seg_base[d1] - g0;
+    }
     const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
     const uint32_t b0 = g0 + min(total, blockIdx.x * per), b1 = g0 + min(total, (blockIdx.x + 1) * per);
     if (threadIdx.x == 0) s_next = b0;
     __syncthreads();
     for (;;) {
-        const uint32_t g = atomicAdd(&s_next, 1u);
-        if (g >= b1) break;
+        const uint32_t q = atomicAdd(&s_next, 1u);
+        if (q >= b1) break;
+        const uint32_t win = kBatch ? window_of(s_pre, nwin, q) : 0u;
+        const WinDev &w = ws.get(win);
+        const uint32_t g = kBatch ? q - s_pre[win] + w.seg_base[d0] : q;
         // driver owning segment g: last i in [d0, d1) with seg_base[i] <= g
         uint32_t lo = d0, hi = d1;
         while (hi - lo > 1) {
@@ -904,25 +996,37 @@ __device__ void sim_segment_warp(const WinDev &w, const LevelArgs &a, const DrvM
 // Warp-per-segment launch for the 1-, 2- and 3-input classes: each block
 // owns a contiguous share of the class's segments and its warps take the
 // next one from a shared counter as they finish.
-template <int M>
-__global__ void __launch_bounds__(128, M == 1 ? 8 : (M == 2 ? 7 : 6)) k_sim_warp(WinDev w, LevelArgs a, uint32_t d0, uint32_t d1)
+template <int M, bool kBatch>
+__global__ void __launch_bounds__(128, M == 1 ? 8 : (M == 2 ? 7 : 6))
+    k_sim_warp(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     constexpr int kWarps = 4;
     __shared__ uint32_t s_next;
     __shared__ WarpSmem<M> sm[kWarps];
-    if (*w.err) return;
-    const uint32_t g0 = w.seg_base[d0], g1 = w.seg_base[d1];
-    const uint32_t total = g1 - g0;
+    __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
+    __shared__ uint32_t sm32[32];
+    const uint32_t nwin = ws.size();
+    uint32_t g0 = 0, total;
+    if (kBatch) {
+        total = window_prefix<false>(
+            ws, [&](const WinDev &x) { return x.seg_base[d1] - x.seg_base[d0]; }, s_pre, sm32);
+    } else {
+        g0 = ws.get(0).seg_base[d0];
+        total = ws.get(0).seg_base[d1] - g0;
+    }
     const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
     const uint32_t b0 = g0 + min(total, blockIdx.x * per), b1 = g0 + min(total, (blockIdx.x + 1) * per);
     if (threadIdx.x == 0) s_next = b0;
     __syncthreads();
     const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     for (;;) {
-        uint32_t g = 0;
-        if (lane == 0) g = atomicAdd(&s_next, 1u);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= b1) break;
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(&s_next, 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= b1) break;
+        const uint32_t win = kBatch ? window_of(s_pre, nwin, q) : 0u;
+        const WinDev &w = ws.get(win);
+        const uint32_t g = kBatch ? q - s_pre[win] + w.seg_base[d0] : q;
         uint32_t lo = d0, hi = d1;
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
@@ -954,13 +1058,16 @@ __device__ __forceinline__ void saif_add(unsigned long long acc[3], int cls, uns
 // pass B drops a segment's first entry when it repeats the last kept value
 // before it, places the segments back to back in the gate's pool slot and
 // hands each segment's copy to k_copy with the final event that precedes it.
-__global__ void __launch_bounds__(256) k_link(WinDev w, LevelArgs a)
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs a)
 {
-    if (*w.err) return;
     const uint32_t n = a.hi - a.lo;
-    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (i >= n) return;
+    if (gw >= (uint64_t)n * ws.size()) return;
+    const uint32_t i = (uint32_t)(gw % n);
+    const WinDev &w = ws.get((uint32_t)(gw / n));
+    if (*w.err) return;
     const unsigned FULL = 0xffffffffu;
     const uint32_t sb = w.seg_base[i], se = w.seg_base[i + 1];
     const uint64_t slot = w.slot[i];
@@ -1099,24 +1206,38 @@ __device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, 
 // level scratch into the pool and add their SAIF contributions to the gate
 // output's counters.  The next segment's record is loaded while the current
 // one is copied.
-__global__ void __launch_bounds__(256) k_copy(WinDev w, LevelArgs a)
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs a)
 {
     constexpr int W = 16;
     const unsigned FULL = 0xffffffffu;
-    if (*w.err) return;
+    __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
+    __shared__ uint32_t sm32[32];
+    const uint32_t nwin = ws.size();
+    // no flag changes during this kernel: windows that failed are left out
+    const uint32_t nseg = window_prefix<true>(ws, [](const WinDev &x) { return *x.n_segs; }, s_pre, sm32);
     const int sub = threadIdx.x & (W - 1);
-    const uint32_t nseg = *w.n_segs;
     const uint32_t gpb = blockDim.x / W;
     const uint32_t stride = gridDim.x * gpb;
     uint32_t s = blockIdx.x * gpb + threadIdx.x / W;
     // every group of a warp runs the same number of rounds (shuffles need the full warp)
     const uint32_t warp_first = blockIdx.x * gpb + (threadIdx.x & ~31u) / W;
     const uint32_t rounds = warp_first < nseg ? (nseg - warp_first + stride - 1) / stride : 0;
-    CopyRec c = {0, 0, 0, 0, 0, 0, 0};
-    if (s < nseg) c = w.copies[s];
+    auto fetch = [&](uint32_t q, uint32_t &win) {
+        CopyRec c = {0, 0, 0, 0, 0, 0, 0};
+        win = 0;
+        if (q < nseg) {
+            win = window_of(s_pre, nwin, q);
+            c = ws.get(win).copies[q - s_pre[win]];
+        }
+        return c;
+    };
+    uint32_t cw;
+    CopyRec c = fetch(s, cw);
     for (uint32_t r = 0; r < rounds; ++r, s += stride) {
-        CopyRec nx = {0, 0, 0, 0, 0, 0, 0};
-        if (s + stride < nseg) nx = w.copies[s + stride];
+        uint32_t nw;
+        const CopyRec nx = fetch(s + stride, nw);
+        const WinDev &w = ws.get(cw);
         const bool live = s < nseg && c.n > 0;
         unsigned long long acc[3] = {0, 0, 0};
         unsigned long long cprev = c.cprev;
@@ -1148,16 +1269,20 @@ __global__ void __launch_bounds__(256) k_copy(WinDev w, LevelArgs a)
                 if (acc[k]) atomicAdd(&w.saif[3ull * out_net + k], acc[k]);
         }
         c = nx;
+        cw = nw;
     }
 }
 
 // ------------------------------------------------------- stimulus SAIF
-__global__ void __launch_bounds__(256) k_stim_saif(WinDev w, const uint32_t *__restrict__ nets, uint32_t n)
+// one warp per stimulus net; blockIdx.y is the window
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_stim_saif(const WinSet<kBatch> ws)
 {
+    const WinDev &w = ws.get(blockIdx.y);
     const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (i >= n) return;
-    const uint32_t net = nets[i];
+    if (i >= w.n_stim) return;
+    const uint32_t net = w.stim_nets[i];
     const uint64_t off = w.net_off[net];
     const uint32_t len = w.net_len[net];
     unsigned long long cprev = w.t_begin;
@@ -1180,48 +1305,69 @@ __global__ void __launch_bounds__(256) k_stim_saif(WinDev w, const uint32_t *__r
     }
 }
 
-void launch_stim_saif(const WinDev &w, const uint32_t *stim_nets, uint32_t n_stim, cudaStream_t st)
+// One window goes by value, several through the device array dw.
+#define GLS_DISPATCH(h, dw, nwin, LAUNCH)                       \
+    do {                                                         \
+        if ((nwin) == 1) {                                       \
+            const WinSet<false> ws{h};                           \
+            LAUNCH;                                              \
+        } else {                                                 \
+            const WinSet<true> ws{dw, nwin};                     \
+            LAUNCH;                                              \
+        }                                                        \
+    } while (0)
+
+void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, cudaStream_t st)
 {
-    if (!n_stim) return;
-    const uint32_t blocks = (uint32_t)(((uint64_t)n_stim * 32 + 255) / 256);
-    k_stim_saif<<<blocks, 256, 0, st>>>(w, stim_nets, n_stim);
+    if (!max_stim || !nwin) return;
+    const dim3 grid((uint32_t)(((uint64_t)max_stim * 32 + 255) / 256), nwin);
+    GLS_DISPATCH(h, dw, nwin, (k_stim_saif<<<grid, 256, 0, st>>>(ws)));
 }
 
-void launch_plan(const WinDev &w, const LevelArgs &a, cudaStream_t st)
+void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
 {
-    k_plan<<<1, 1024, 0, st>>>(w, a);
+    GLS_DISPATCH(h, dw, nwin, (k_plan<<<nwin, 1024, 0, st>>>(ws, a)));
 }
 
-void launch_sim(const WinDev &w, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count, cudaStream_t st)
+template <class WS>
+static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
+                        cudaStream_t st)
 {
+    constexpr bool B = std::is_same<WS, WinSet<true>>::value;
     if ((a.warp_mask >> cls) & 1u) {
         const int wgrid = sm_count * 8;
         switch (cls) {
-        case 0: k_sim_warp<1><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
-        case 1: k_sim_warp<2><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
-        case 2: k_sim_warp<3><<<wgrid, 128, 0, st>>>(w, a, d0, d1); return;
+        case 0: k_sim_warp<1, B><<<wgrid, 128, 0, st>>>(ws, a, d0, d1); return;
+        case 1: k_sim_warp<2, B><<<wgrid, 128, 0, st>>>(ws, a, d0, d1); return;
+        case 2: k_sim_warp<3, B><<<wgrid, 128, 0, st>>>(ws, a, d0, d1); return;
         default: break;
         }
     }
     const int grid = sm_count * (cls <= 1 ? 8 : (cls == 2 ? 6 : 4));
     switch (cls) {
-    case 0: k_sim<1><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
-    case 1: k_sim<2><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
-    case 2: k_sim<3><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
-    default: k_sim<kMaxSlots><<<grid, 128, 0, st>>>(w, a, d0, d1); break;
+    case 0: k_sim<1, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
+    case 1: k_sim<2, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
+    case 2: k_sim<3, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
+    default: k_sim<kMaxSlots, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
     }
 }
 
-void launch_link(const WinDev &w, const LevelArgs &a, cudaStream_t st)
+void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,
+                int sm_count, cudaStream_t st)
 {
-    const uint32_t n = a.hi - a.lo;
-    const uint32_t blocks = (uint32_t)(((uint64_t)n * 32 + 255) / 256);
-    k_link<<<blocks, 256, 0, st>>>(w, a);
+    GLS_DISPATCH(h, dw, nwin, sim_kernels(ws, a, cls, d0, d1, sm_count, st));
 }
 
-void launch_copy(const WinDev &w, const LevelArgs &a, int sm_count, cudaStream_t st)
+void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
 {
-    k_copy<<<sm_count * 8, 256, 0, st>>>(w, a);
+    const uint64_t warps = (uint64_t)(a.hi - a.lo) * nwin;
+    const uint32_t blocks = (uint32_t)((warps * 32 + 255) / 256);
+    GLS_DISPATCH(h, dw, nwin, (k_link<<<blocks, 256, 0, st>>>(ws, a)));
+}
+
+void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st)
+{
+    GLS_DISPATCH(h, dw, nwin, (k_copy<<<sm_count * 8, 256, 0, st>>>(ws, a)));
 }
 
 }  // namespace gls

@@ -90,6 +90,20 @@ __device__ __forceinline__ uint32_t reserve_of(const PresizeArgs &a, float y)
     return r >= 4.0e9f ? 0xFFFFFFF0u : (uint32_t)r;
 }
 
+// the window's own buffers when the rows are gate outputs of a batch of windows
+__device__ __forceinline__ PresizeArgs for_window(const PresizeArgs &a)
+{
+    PresizeArgs b = a;
+    if (a.wv) {
+        const WinDev &w = a.wv[blockIdx.y];
+        b.net_len = w.net_len;
+        b.saif = w.saif;
+        b.pred = w.pred;
+        b.err = w.err;
+    }
+    return b;
+}
+
 __global__ void __launch_bounds__(256) k_features(PresizeArgs a, float *out)
 {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,8 +116,9 @@ __global__ void __launch_bounds__(256) k_features(PresizeArgs a, float *out)
 
 // ------------------------------------------------ FP32 CUDA-core inference
 // One thread per row; the FP32 weights sit in shared memory.
-__global__ void __launch_bounds__(128) k_presize_f32(PresizeArgs a)
+__global__ void __launch_bounds__(128) k_presize_f32(PresizeArgs a0)
 {
+    const PresizeArgs a = for_window(a0);
     extern __shared__ float sp[];
     for (uint32_t k = threadIdx.x; k < (uint32_t)kParams; k += blockDim.x) sp[k] = a.params[k];
     __syncthreads();
@@ -213,8 +228,9 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__global__ void __launch_bounds__(128, 1) k_presize_tc(PresizeArgs a)
+__global__ void __launch_bounds__(128, 1) k_presize_tc(PresizeArgs a0)
 {
+    const PresizeArgs a = for_window(a0);
     extern __shared__ __align__(1024) uint8_t sm[];
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
@@ -333,25 +349,20 @@ void launch_features(const PresizeArgs &a, float *out, cudaStream_t st)
     k_features<<<(a.n + 255) / 256, 256, 0, st>>>(a, out);
 }
 
+// the dynamic shared-memory limits of both inference kernels (the current
+// device; called before any launch and outside stream capture)
+void prepare_presize_kernels()
+{
+    cudaFuncSetAttribute(k_presize_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
+    cudaFuncSetAttribute(k_presize_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kParams * 4));
+}
+
 void launch_presize(const PresizeArgs &a, bool tensor_cores, cudaStream_t st)
 {
     if (!a.n) return;
-    const uint32_t grid = (a.n + 127) / 128;
-    if (tensor_cores) {
-        static bool attr = false;   // per process; the attribute holds for every device
-        if (!attr) {
-            cudaFuncSetAttribute(k_presize_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmTotal);
-            attr = true;
-        }
-        k_presize_tc<<<grid, 128, kSmTotal, st>>>(a);
-    } else {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_presize_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kParams * 4));
-            attr = true;
-        }
-        k_presize_f32<<<grid, 128, kParams * 4, st>>>(a);
-    }
+    const dim3 grid((a.n + 127) / 128, a.wv ? a.nwin : 1);
+    if (tensor_cores) k_presize_tc<<<grid, 128, kSmTotal, st>>>(a);
+    else k_presize_f32<<<grid, 128, kParams * 4, st>>>(a);
 }
 
 // ------------------------------------------------------------- training
@@ -798,6 +809,8 @@ extern "C" int gls_set_presize_model(gls_ctx *ctx, const gls_presize_model *m)
     ctx->margin = m->margin;
     ctx->slack = m->slack;
     ctx->have_model = true;
+    ctx_drop_graphs(ctx);
+    prepare_presize_kernels();
     return GLS_OK;
 }
 
@@ -867,6 +880,7 @@ extern "C" int gls_presize_predict(gls_ctx *ctx, const gls_presize_model *m, con
     if (e == cudaSuccess) e = cudaMemcpy(im.p, img.data(), kImgBytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(rows.p, feat, n * kIn * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(er.p, 0, 16);
+    prepare_presize_kernels();
     uint32_t flag = 0;
     if (e == cudaSuccess) {
         PresizeArgs a;

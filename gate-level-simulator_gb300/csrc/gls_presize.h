@@ -27,6 +27,8 @@ struct PresizeArgs {
     // rows: either host-supplied feature rows, or gate outputs [lo, lo + n)
     // whose features are the static row plus the input-net lengths
     const float *rows;            // n x 32, or null
+    const WinDev *wv;             // windows (blockIdx.y) supplying net_len, saif, pred, err; or null
+    uint32_t nwin;
     const float *feat_static;     // per driver x 32
     const DrvMeta *meta;
     const uint8_t *lut;           // cell truth tables
@@ -42,6 +44,7 @@ struct PresizeArgs {
     uint32_t *err;                // set on a tensor-core wait timeout
 };
 
+void prepare_presize_kernels();
 void launch_presize(const PresizeArgs &a, bool tensor_cores, cudaStream_t st);
 void launch_features(const PresizeArgs &a, float *out, cudaStream_t st);
 

@@ -15,6 +15,7 @@
 // scratch lives differs.
 #include <cuda_runtime.h>
 #include <cstdio>
+#include <cstring>
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -33,7 +34,8 @@ constexpr uint64_t kStaticMaxWords = 4194304;        // segment-stack words per 
 // Layout of the static scratch (byte offsets, each 256-byte aligned).
 constexpr uint64_t al256(uint64_t x) { return (x + 255) & ~255ull; }
 constexpr uint64_t kOffSmall = 0;                                            // 8 x u64: err, counters, n_segs
-constexpr uint64_t kOffSegBase = al256(kOffSmall + 64);
+constexpr uint64_t kOffWin = 64;                                             // the level kernels' WinDev
+constexpr uint64_t kOffSegBase = al256(kOffWin + sizeof(WinDev));
 constexpr uint64_t kOffSlot = al256(kOffSegBase + 4ull * (kStaticMaxOutputs + 1));
 constexpr uint64_t kOffScr = al256(kOffSlot + 8ull * (kStaticMaxOutputs + 1));
 constexpr uint64_t kOffSegs = al256(kOffScr + 8ull * (kStaticMaxOutputs + 1));
@@ -107,6 +109,7 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     e = cudaMemsetAsync(small, 0, 64, ctx->stream);
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "clear static flags: %s", cudaGetErrorString(e));
     WinDev d;
+    std::memset(&d, 0, sizeof d);
     d.net_off = d_net_off;
     d.net_len = d_net_len;
     d.pool = d_pool;
@@ -116,7 +119,6 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     d.err = reinterpret_cast<uint32_t *>(small + 5);
     d.n_segs = reinterpret_cast<uint32_t *>(small + 6);
     d.n_over = small + 7;
-    d.res = nullptr;
     d.seg_base = reinterpret_cast<uint32_t *>(base + kOffSegBase);
     d.slot = reinterpret_cast<uint64_t *>(base + kOffSlot);
     d.scr = reinterpret_cast<uint64_t *>(base + kOffScr);
@@ -131,18 +133,21 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     LevelArgs a;
     ctx_level_args(ctx, &a);
     a.alloc_mode = kAllocBound;   // the caller's pool: slots reserved up front
-    a.pred = nullptr;
     a.lo = lo + first;
     a.hi = a.lo + count;
-    launch_plan(d, a, ctx->stream);
+    // the descriptor goes into its slot of the static array (no allocation)
+    WinDev *dw = reinterpret_cast<WinDev *>(base + kOffWin);
+    e = cudaMemcpyAsync(dw, &d, sizeof d, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "upload static descriptor: %s", cudaGetErrorString(e));
+    launch_plan(dw, d, 1, a, ctx->stream);
     for (int c = 0; c < kClasses; ++c) {
         // the fan-in class ranges of the level, clipped to [first, first + count)
         const uint32_t c0 = ctx->cls_start[(kClasses + 1) * level + c], c1 = ctx->cls_start[(kClasses + 1) * level + c + 1];
         const uint32_t d0 = std::max(c0, first), d1 = std::min(c1, first + count);
-        if (d1 > d0) launch_sim(d, a, c, d0 - first, d1 - first, ctx->sm_count, ctx->stream);
+        if (d1 > d0) launch_sim(dw, d, 1, a, c, d0 - first, d1 - first, ctx->sm_count, ctx->stream);
     }
-    launch_link(d, a, ctx->stream);
-    launch_copy(d, a, ctx->sm_count, ctx->stream);
+    launch_link(dw, d, 1, a, ctx->stream);
+    launch_copy(dw, d, 1, a, ctx->sm_count, ctx->stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "level kernel launch: %s", cudaGetErrorString(e));
     unsigned long long st[8];

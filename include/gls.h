@@ -168,8 +168,20 @@ int gls_add_window(gls_ctx *ctx, const gls_stimulus *stim, uint64_t t_begin,
 int gls_clear_windows(gls_ctx *ctx);
 
 /* Simulate every added window through all levels.  Replaces the per-level
- * loop src/simulate.cu:2027-3254 (merge, SimulateCuda, compaction, D2H). */
+ * loop src/simulate.cu:2027-3254 (merge, SimulateCuda, compaction, D2H).
+ * Windows run one after the other. */
 int gls_run(gls_ctx *ctx);
+
+/* Batched windows (no counterpart in the reference, which takes one VCD
+ * window per process): the added windows run in waves, each level of a wave
+ * one launch per kernel over all its windows; results equal gls_run's. */
+typedef struct {
+    uint32_t max_wave;   /* windows per wave (0: all, or as many as device memory holds with saif_only) */
+    int use_graph;       /* 1: capture a wave's launches once as a CUDA graph and replay it for every wave */
+    int saif_only;       /* 1: free each window's event pool after its wave; SAIF counts and list lengths
+                            stay readable, gls_waveform does not */
+} gls_batch_opts;
+int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts);
 
 /* T0 / T1 / TX per net for a window (arrays of n_nets).  Nets the run did
  * not produce read UINT64_MAX.  Replaces the SAIF integrals of
