@@ -32,10 +32,13 @@ sys.path[:0] = [str(REPO), str(REPO / "gate-level-simulator_gb300")]
 
 import numpy as np  # noqa: E402
 
+C4_WINDOWS, C4_MIN_CYCLES, C4_MAX_CYCLES = 256, 1_000, 50_000
+
 WORKLOADS = {
     "c1": "c1: 2,000 cells, depth 20, 192 pseudo-primary inputs, 1,000 cycles of 1,000 ps, p=0.2",
     "c2": "c2: 200,000 cells, depth 60, 4,096 pseudo-primary inputs, 10,000 cycles of 1,000 ps, p~Beta(2,8)",
     "c3": "c3: 2,000,000 cells, depth 120, 65,536 pseudo-primary inputs, 20,000 cycles of 1,000 ps, p log-uniform [0.01,0.5]",
+    "c4": "c4: the c2 netlist with 256 windows of U[1,000, 50,000] cycles, each with its own seed and Beta(2,8) rates",
 }
 
 
@@ -106,7 +109,7 @@ def peak_hbm():
 
 def make_workload(name: str, seed: int, cells=None, depth=None, cycles=None):
     from gls import synth
-    cfg = synth.CONFIGS[name]
+    cfg = synth.CONFIGS["c2" if name == "c4" else name]
     if cells or depth or cycles:
         cfg = synth.scaled(cfg, cells=cells, depth=depth, cycles=cycles)
     t0 = time.time()
@@ -357,6 +360,106 @@ def gls_arm(args):
         torch.distributed.destroy_process_group()
 
 
+def batched_arm(args):
+    """c4: many windows of uneven length on one netlist.  One step simulates
+    all windows with gls_run_batched (waves of windows, one launch per kernel
+    and level over a wave, graph replay, pools freed after each wave); the
+    same windows as sequential plain runs (one gls_run each, exact
+    allocation) are timed beside it."""
+    import torch
+    from gls import synth
+    from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED, Simulator
+    from gls.netlist import Stimulus
+    torch.cuda.set_device(0)
+    cfg, nl = make_workload("c2", args.seed, args.cells, args.depth, None)
+    rng = np.random.default_rng(args.seed + 4)
+    n_win = args.windows or C4_WINDOWS
+    lengths = rng.integers(C4_MIN_CYCLES, C4_MAX_CYCLES + 1, size=n_win)
+    t0 = time.time()
+    wins = []
+    for k, cyc in enumerate(lengths.tolist()):
+        c = synth.scaled(cfg, cycles=int(cyc))
+        st = synth.make_stimulus(c, nl.ppi_nets, seed=args.seed + 100 + k)
+        # pinned host copies: the end-to-end leg uploads from them
+        p = {f: torch.from_numpy(np.ascontiguousarray(getattr(st, f))).pin_memory().numpy()
+             for f in ("nets", "ev_start", "time", "value")}
+        wins.append((Stimulus(p["nets"], p["ev_start"], p["time"], p["value"]), c.t_end))
+    log(f"c4: {n_win} windows, {int(lengths.sum())} cycles, "
+        f"{sum(len(w[0].time) for w in wins)} stimulus events ({time.time() - t0:.1f}s)")
+    alloc = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}[args.alloc]
+
+    def batched_pass(sim):
+        sim.clear_windows()
+        for st, t_end in wins:
+            sim.add_window(st, 0, t_end)
+        sim.run_batched(saif_only=True)
+        return [sim.saif(k) for k in range(len(wins))]
+
+    sim = Simulator(alloc_mode=alloc)
+    if args.alloc == "learned":
+        from gls import presize
+        sim.set_presize_model(presize.load(args.model or presize.DEFAULT_MODEL))
+    sim.load(nl)
+    for st, t_end in wins:
+        sim.add_window(st, 0, t_end)
+    tune = sim.autotune(saif_only=True)   # untimed: picks the schedule on the first wave
+    log(f"autotune: {tune['best']} over {tune['windows']} windows")
+    for _ in range(args.warmup):
+        batched_pass(sim)
+    stats = sim.stats()
+    gate_ev = stats["gate_events"]
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for _ in range(args.steps):
+            batched_pass(sim)
+            dev_ms += sim.stats()["kernel_ms"]
+        torch.cuda.synchronize()
+        step_s = (time.perf_counter() - t0) / args.steps
+    dev_s = dev_ms / 1000.0 / args.steps
+    launches = sim.stats()["launches"]
+    pool_b = sim.stats()["pool_bytes"]
+    sim.close()
+    # sequential plain runs of the same windows (exact allocation, one gls_run each)
+    plain = Simulator(alloc_mode=ALLOC_EXACT)
+    plain.load(nl)
+    plain_s = 0.0
+    for rep in range(2):   # the first pass warms up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for st, t_end in wins:
+            plain.clear_windows()
+            w = plain.add_window(st, 0, t_end)
+            plain.run()
+            plain.saif(w)
+        torch.cuda.synchronize()
+        plain_s = time.perf_counter() - t0
+    plain.close()
+    line = {
+        "metric": "gate-events/s", "value": gate_ev / dev_s, "unit": "gate-events/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": workload_desc(args), "seed": args.seed, "windows": n_win,
+                   "cycles": int(lengths.sum()), "alloc": args.alloc, "parallelism": "replicas x1",
+                   "l2": "every step streams GBs of event pool per window (> L2)",
+                   "schedule": tune["best"], "value_timing": "device time of the waves (stimulus uploads "
+                   "between waves excluded); e2e: wall clock of add_window + run_batched + SAIF reads"},
+        "sim_cycles_per_s": float(lengths.sum()) / dev_s,
+        "gate_events_per_step": gate_ev,
+        "e2e": {"value": gate_ev / step_s, "unit": "gate-events/s",
+                "h2d_bytes_per_step": int(sum(st.time.nbytes + st.value.nbytes for st, _ in wins)),
+                "d2h_bytes_per_step": int(24 * nl.n_nets * n_win), "ms_per_step": 1000.0 * step_s},
+        "plain_sequential": {"value": gate_ev / plain_s, "unit": "gate-events/s", "ms": 1000.0 * plain_s,
+                             "what": f"{n_win} sequential gls_run calls, exact allocation, wall clock"},
+        "batched_over_plain": plain_s / step_s,
+        "gpu_launches": int(launches),
+        "pool_bytes": pool_b,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -373,12 +476,15 @@ def main():
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling cases)")
     ap.add_argument("--depth", type=int, default=None, help="override the logic depth (profiling cases)")
     ap.add_argument("--cycles", type=int, default=None, help="override the cycle count (profiling cases)")
+    ap.add_argument("--windows", type=int, default=None, help="c4: number of windows (default 256)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
     if args.impl == "reference":
         reference_arm(args)
+    elif args.config == "c4":
+        batched_arm(args)
     else:
         gls_arm(args)
 

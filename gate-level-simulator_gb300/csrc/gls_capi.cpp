@@ -57,7 +57,7 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->lut = ctx->lut.as<uint8_t>();
     a->lo = a->hi = 0;
     a->seg_events = ctx->opts.seg_events;
-    a->seg_target = (uint32_t)ctx->sm_count * 2048u;
+    a->seg_target = (uint32_t)ctx->sm_count * ctx->seg_per_sm;
     a->seg_target_w = ctx->seg_target_w;
     a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
@@ -427,9 +427,31 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
     return GLS_OK;
 }
 
+// mean stimulus list length x input pins: what the gate-output pool scales with
+static double pool_scale(const gls_ctx *ctx, const Window *w)
+{
+    const double avg = w->stim_nets.empty() ? 4.0 : (double)w->stim_events / (double)w->stim_nets.size();
+    return avg * (double)ctx->pins_total;
+}
+
+// the pool a window is given: its estimate, raised to what earlier windows
+// of this netlist needed (unless the caller fixed the size)
+static uint64_t projected_cap(const gls_ctx *ctx, const Window *w)
+{
+    uint64_t cap = w->cap;
+    if (!ctx->opts.pool_events && ctx->pool_ratio > 0.0) {
+        const uint64_t need = w->stim_events + ctx->pool_gap + 8ull * ctx->n_drv + 1024 +
+                              (uint64_t)(1.1 * ctx->pool_ratio * pool_scale(ctx, w));
+        cap = std::max(cap, need);
+    }
+    return cap;
+}
+
 static int upload_window(gls_ctx *ctx, Window *w)
 {
     const uint64_t n = ctx->n_nets;
+    if (w->pool.bytes < projected_cap(ctx, w) * 4) w->pool.release();
+    w->cap = std::max(w->cap, projected_cap(ctx, w));
     CK(w->pool.ensure(w->cap * 4), "alloc event pool");
     CK(w->net_off.ensure(n * 8), "alloc net_off");
     CK(w->net_len.ensure(n * 4), "alloc net_len");
@@ -546,8 +568,11 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     // initial pool capacity: stimulus plus an estimate of every gate's slot
     uint64_t cap = ctx->opts.pool_events;
     if (!cap) {
+        // gate outputs take about as many events as one input on average; an
+        // upper-bound slot reserves the sum over the inputs
         const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
-        cap = total + (uint64_t)(1.5 * avg * (double)ctx->pins_total) + 8ull * ctx->n_drv + 1024;
+        const double f = ctx->opts.alloc_mode == GLS_ALLOC_BOUND ? 2.5 : 1.3;
+        cap = total + (uint64_t)(f * avg * (double)ctx->pins_total) + 8ull * ctx->n_drv + 1024;
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
             const uint64_t limit = (uint64_t)(fr * 0.6) / 5;
@@ -558,7 +583,8 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     // level scratch: the widest level's fan-in events, estimated from the stimulus
     {
         const double avg = st->n_nets ? (double)total / st->n_nets : 4.0;
-        uint64_t want = (uint64_t)(2.0 * avg * 6.0 * ctx->max_width) + 16ull * ctx->max_width + 4096;
+        const double fan = std::max(1.0, (double)ctx->pins_total / std::max<uint32_t>(1, ctx->n_drv));
+        uint64_t want = (uint64_t)(2.0 * avg * fan * ctx->max_width) + 16ull * ctx->max_width + 4096;
         if (want > ctx->scr_cap) {
             ctx->scr_cap = want;
             CK(ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level scratch");
@@ -710,6 +736,10 @@ static int settle_window(gls_ctx *ctx, Window *w, RunAcc &acc)
         CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
         const uint32_t err = (uint32_t)small[5];
         if (!err) {
+            const double sc = pool_scale(ctx, w);
+            if (sc > 0.0 && small[0] > w->stim_events + ctx->pool_gap)
+                ctx->pool_ratio = std::max(ctx->pool_ratio,
+                                           (double)(small[0] - w->stim_events - ctx->pool_gap) / sc);
             acc.over_ev += small[7];
             acc.gate_ev += small[1];
             acc.out_ev += small[2];
@@ -730,7 +760,12 @@ static int settle_window(gls_ctx *ctx, Window *w, RunAcc &acc)
         if (attempt > 12) return fail(ctx, GLS_EOVERFLOW, "event pool could not grow enough");
         if (err & kErrSegCap) ctx->seg_cap = std::max<uint32_t>(ctx->seg_cap, ctx->lsc[0]->seg_cap) * 2;
         if (err & kErrScratch) ctx->scr_cap = std::max<uint64_t>(ctx->scr_cap, ctx->lsc[0]->scr_cap) * 2;
-        CK(ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "grow level work space");
+        {
+            const cudaError_t e = ctx->lsc[0]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap);
+            if (e != cudaSuccess)
+                return fail(ctx, GLS_ENOMEM, "grow level work space to %llu stack words / %u segments (flags 0x%x): %s",
+                            (unsigned long long)ctx->scr_cap, ctx->seg_cap, err, cudaGetErrorString(e));
+        }
         if (err & kErrPool) {
             w->cap *= 2;
             w->pool.release();
@@ -826,116 +861,220 @@ extern "C" int gls_run(gls_ctx *ctx)
     return GLS_OK;
 }
 
-extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
+// Checks and buffers of a batched run; *B receives the windows per wave.
+static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
 {
-    if (!ctx) return GLS_EINVAL;
     if (!ctx->loaded) return fail(ctx, GLS_ESTATE, "run before load_netlist");
     if (ctx->opts.alloc_mode == GLS_ALLOC_LEARNED && !ctx->have_model)
         return fail(ctx, GLS_ESTATE, "GLS_ALLOC_LEARNED needs gls_set_presize_model before gls_run_batched");
-    gls_batch_opts o{0, 1, 0};
-    if (opts) o = *opts;
     cudaSetDevice(ctx->opts.device);
     const size_t nw = ctx->windows.size();
-    RunAcc acc;
-    const double kms[4] = {0, 0, 0, 0};
-    if (!nw) {
-        publish_stats(ctx, acc, kms);
-        return GLS_OK;
-    }
     if (o.saif_only)
         for (Window *w : ctx->windows) release_window_pool(w);
     // windows per wave: all of them, or with saif_only as many as free device
     // memory holds (each needs its pool, net tables and a level work space)
-    uint64_t B = std::min<uint64_t>(nw, kMaxWave);
-    if (o.max_wave) B = std::min<uint64_t>(B, o.max_wave);
+    uint64_t b = std::min<uint64_t>(std::max<size_t>(nw, 1), kMaxWave);
+    if (o.max_wave) b = std::min<uint64_t>(b, o.max_wave);
     if (o.saif_only) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
         uint64_t per = 0;
-        for (Window *w : ctx->windows) per = std::max<uint64_t>(per, w->cap * 4);
+        for (Window *w : ctx->windows) per = std::max<uint64_t>(per, projected_cap(ctx, w) * 4);
         per += (uint64_t)ctx->n_nets * 48 + (uint64_t)(ctx->max_width + 1) * 32 +
                (uint64_t)ctx->seg_cap * (sizeof(SegRec) + sizeof(CopyRec)) + ctx->scr_cap * 4;
         const uint64_t fit = std::max<uint64_t>(1, (uint64_t)(0.85 * (double)fr) / std::max<uint64_t>(per, 1));
-        B = std::max<uint64_t>(1, std::min(B, fit));
+        b = std::max<uint64_t>(1, std::min(b, fit));
     }
-    while (ctx->lsc.size() < B) ctx->lsc.push_back(new LevelScratch);
-    for (uint64_t k = 0; k < B; ++k)
+    while (ctx->lsc.size() < b) ctx->lsc.push_back(new LevelScratch);
+    for (uint64_t k = 0; k < b; ++k)
         CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
     if (!ctx->hwave.ensure(kMaxWave * sizeof(WinDev))) return fail(ctx, GLS_ENOMEM, "pinned wave descriptors");
     CK(ctx->dwave.ensure(kMaxWave * sizeof(WinDev)), "alloc wave descriptors");
+    *B = b;
+    return GLS_OK;
+}
+
+// One wave: windows [w0, w0 + nwin) together; *ms receives its device time
+// (upload of new stimuli excluded, reruns of windows that outgrew a buffer
+// included in acc).
+static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts &o, RunAcc &acc, float *ms,
+                    cudaEvent_t e0, cudaEvent_t e1)
+{
     WinDev *hw = ctx->hwave.as<WinDev>();
+    uint32_t max_stim = 0;
+    for (uint32_t k = 0; k < nwin; ++k)
+        CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
+    for (uint32_t k = 0; k < nwin; ++k) {
+        Window *w = ctx->windows[w0 + k];
+        int rc = w->uploaded ? GLS_OK : upload_window(ctx, w);
+        if (rc == GLS_OK) rc = reset_window(ctx, w);
+        if (rc) return rc;
+        w->saif_only = false;
+        hw[k] = make_windev(ctx, w, *ctx->lsc[k]);
+        max_stim = std::max(max_stim, hw[k].n_stim);
+    }
+    CK(cudaEventRecord(e0, ctx->stream), "event");
+    CK(cudaMemcpyAsync(ctx->dwave.p, hw, nwin * sizeof(WinDev), cudaMemcpyHostToDevice, ctx->stream),
+       "upload wave descriptors");
+    const WinDev *dw = ctx->dwave.as<WinDev>();
+    if (o.use_graph && nwin > 1) {
+        // one graph per wave shape; the descriptors it reads are rewritten per wave
+        const uint64_t key = (uint64_t)nwin | ((uint64_t)max_stim << 11) | ((uint64_t)ctx->warp_mask << 43) |
+                             ((uint64_t)ctx->opts.alloc_mode << 46) | ((uint64_t)ctx->seg_per_sm << 48);
+        cudaGraphExec_t ge = nullptr;
+        uint32_t l = 0;
+        for (auto &g : ctx->graphs)
+            if (g.key == key) {
+                ge = g.exec;
+                l = g.launches;
+            }
+        if (!ge) {
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+            int rc = GLS_OK;
+            if (e == cudaSuccess) {
+                rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &l);
+                const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+                if (rc == GLS_OK && e2 != cudaSuccess) e = e2;
+            }
+            if (rc == GLS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+            if (g) cudaGraphDestroy(g);
+            if (rc) return rc;
+            if (e != cudaSuccess) return fail(ctx, GLS_ECUDA, "capture wave graph: %s", cudaGetErrorString(e));
+            ctx->graphs.push_back({key, ge, l});
+        }
+        CK(cudaGraphLaunch(ge, ctx->stream), "graph launch");
+        acc.launches += l;
+    } else {
+        int rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &acc.launches);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(e1, ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "wave");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t;
+    // windows that finished first (and, with saif_only, give their pools
+    // back), then the ones that outgrew a buffer, rerun alone with more room
+    std::vector<uint32_t> again;
+    for (uint32_t k = 0; k < nwin; ++k) {
+        Window *w = ctx->windows[w0 + k];
+        unsigned long long small[8];
+        CK(cudaMemcpy(small, w->small.p, sizeof small, cudaMemcpyDeviceToHost), "read status");
+        if (small[5]) {
+            again.push_back(k);
+            continue;
+        }
+        int rc = settle_window(ctx, w, acc);
+        if (rc) return rc;
+        if (o.saif_only) {
+            release_window_pool(w);
+            w->saif_only = true;
+        }
+    }
+    if (!again.empty())   // room for the reruns: the other windows' work spaces come back next wave
+        for (size_t k = 1; k < ctx->lsc.size(); ++k) ctx->lsc[k]->release();
+    for (uint32_t k : again) {
+        Window *w = ctx->windows[w0 + k];
+        int rc = settle_window(ctx, w, acc);
+        if (rc) return rc;
+        if (o.saif_only) {
+            release_window_pool(w);
+            w->saif_only = true;
+        }
+    }
+    return GLS_OK;
+}
+
+extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
+{
+    if (!ctx) return GLS_EINVAL;
+    gls_batch_opts o{0, 1, 0};
+    if (opts) o = *opts;
+    uint64_t B = 1;
+    int rc = batch_setup(ctx, o, &B);
+    if (rc) return rc;
+    RunAcc acc;
+    const double kms[4] = {0, 0, 0, 0};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
-    float run_ms = 0.f;
-    int rc = GLS_OK;
-    for (size_t w0 = 0; w0 < nw && rc == GLS_OK; w0 += B) {
-        const uint32_t nwin = (uint32_t)std::min<uint64_t>(B, nw - w0);
-        uint32_t max_stim = 0;
-        for (uint32_t k = 0; k < nwin && rc == GLS_OK; ++k) {
-            Window *w = ctx->windows[w0 + k];
-            if (!w->uploaded) rc = upload_window(ctx, w);
-            if (rc == GLS_OK) rc = reset_window(ctx, w);
-            w->saif_only = false;
-            hw[k] = make_windev(ctx, w, *ctx->lsc[k]);
-            max_stim = std::max(max_stim, hw[k].n_stim);
-        }
-        if (rc) break;
-        cudaEventRecord(e0, ctx->stream);
-        cudaError_t e = cudaMemcpyAsync(ctx->dwave.p, hw, nwin * sizeof(WinDev), cudaMemcpyHostToDevice, ctx->stream);
-        if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "upload wave descriptors: %s", cudaGetErrorString(e)); break; }
-        const WinDev *dw = ctx->dwave.as<WinDev>();
-        if (o.use_graph && nwin > 1) {
-            // one graph per wave shape; the descriptors it reads are rewritten per wave
-            const uint64_t key = (uint64_t)nwin | ((uint64_t)max_stim << 11) | ((uint64_t)ctx->warp_mask << 43) |
-                                 ((uint64_t)ctx->opts.alloc_mode << 46);
-            cudaGraphExec_t ge = nullptr;
-            uint32_t l = 0;
-            for (auto &g : ctx->graphs)
-                if (g.key == key) {
-                    ge = g.exec;
-                    l = g.launches;
-                }
-            if (!ge) {
-                cudaGraph_t g = nullptr;
-                e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-                if (e == cudaSuccess) {
-                    rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &l);
-                    const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
-                    if (rc == GLS_OK && e2 != cudaSuccess) e = e2;
-                }
-                if (rc == GLS_OK && e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
-                if (g) cudaGraphDestroy(g);
-                if (rc) break;
-                if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "capture wave graph: %s", cudaGetErrorString(e)); break; }
-                ctx->graphs.push_back({key, ge, l});
+    for (size_t w0 = 0; w0 < ctx->windows.size() && rc == GLS_OK;) {
+        uint64_t nwin = std::min<uint64_t>(B, ctx->windows.size() - w0);
+        if (o.saif_only) {
+            // pools grow with what earlier windows needed: refit the wave to free memory
+            size_t fr = 0, tot = 0;
+            cudaMemGetInfo(&fr, &tot);
+            uint64_t per = 1;
+            for (uint64_t k = 0; k < nwin; ++k) {
+                const Window *w = ctx->windows[w0 + k];
+                per = std::max<uint64_t>(per, projected_cap(ctx, w) * 4 + (uint64_t)ctx->n_nets * 48);
             }
-            e = cudaGraphLaunch(ge, ctx->stream);
-            if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "graph launch: %s", cudaGetErrorString(e)); break; }
-            acc.launches += l;
-        } else {
-            rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &acc.launches);
-            if (rc) break;
+            nwin = std::max<uint64_t>(1, std::min<uint64_t>(nwin, (uint64_t)(0.85 * (double)fr) / per));
         }
-        cudaEventRecord(e1, ctx->stream);
-        e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) { rc = fail(ctx, GLS_ECUDA, "wave: %s", cudaGetErrorString(e)); break; }
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        run_ms += ms;
-        for (uint32_t k = 0; k < nwin && rc == GLS_OK; ++k) rc = settle_window(ctx, ctx->windows[w0 + k], acc);
-        if (o.saif_only)
-            for (uint32_t k = 0; k < nwin; ++k) {
-                Window *w = ctx->windows[w0 + k];
-                release_window_pool(w);
-                w->saif_only = true;
-            }
+        rc = run_wave(ctx, w0, (uint32_t)nwin, o, acc, &ms, e0, e1);
+        acc.total_ms += ms;
+        w0 += nwin;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    acc.total_ms += run_ms;
     publish_stats(ctx, acc, kms);
+    return GLS_OK;
+}
+
+extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_result *res)
+{
+    if (!ctx) return GLS_EINVAL;
+    if (ctx->windows.empty()) return fail(ctx, GLS_ESTATE, "autotune needs at least one added window");
+    gls_batch_opts o{0, 1, 0};
+    if (opts) o = *opts;
+    uint64_t B = 1;
+    int rc = batch_setup(ctx, o, &B);
+    if (rc) return rc;
+    const uint32_t nwin = (uint32_t)std::min<uint64_t>(B, ctx->windows.size());
+    // candidates: time segments per SM for the thread-per-segment kernel, and
+    // which fan-in classes run warp-per-segment
+    static const uint32_t kSegs[] = {1024, 2048, 4096};
+    static const uint32_t kMasks[] = {0, 1, 7};
+    gls_tune_result r;
+    std::memset(&r, 0, sizeof r);
+    float best = 1e30f;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    const uint32_t keep_segs = ctx->seg_per_sm, keep_mask = ctx->warp_mask;
+    for (uint32_t ms_i = 0; ms_i < 3 && rc == GLS_OK; ++ms_i) {
+        for (uint32_t s_i = 0; s_i < 3 && rc == GLS_OK; ++s_i) {
+            ctx->seg_per_sm = kSegs[s_i];
+            ctx->warp_mask = kMasks[ms_i];
+            RunAcc acc;
+            float t = 0.f;
+            // the first run of a shape captures its graph: time the second
+            for (int rep = 0; rep < 2 && rc == GLS_OK; ++rep) rc = run_wave(ctx, 0, nwin, o, acc, &t, e0, e1);
+            const uint32_t c = ms_i * 3 + s_i;
+            r.ms[c] = t;
+            r.seg_per_sm[c] = kSegs[s_i];
+            r.warp_mask[c] = kMasks[ms_i];
+            if (rc == GLS_OK && t < best) {
+                best = t;
+                r.best = c;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r.n = 9;
+    r.windows = nwin;
+    if (rc) {
+        ctx->seg_per_sm = keep_segs;
+        ctx->warp_mask = keep_mask;
+        return rc;
+    }
+    ctx->seg_per_sm = r.seg_per_sm[r.best];
+    ctx->warp_mask = r.warp_mask[r.best];
+    if (res) *res = r;
     return GLS_OK;
 }
 

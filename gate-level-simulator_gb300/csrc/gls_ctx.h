@@ -134,8 +134,10 @@ struct gls_ctx {
     uint64_t scr_cap = 0;                    // stack words new work spaces get
     uint32_t def_delay = 1;
     uint32_t warp_mask = 0;          // fan-in classes run by the warp-per-segment kernel (GLS_SIM_WARP_MASK)
+    uint32_t seg_per_sm = 2048;      // time segments per SM and fan-in class for the thread-per-segment kernel
     uint32_t seg_target_w = 0;       // segments per class for those kernels (GLS_SIM_WARP_SEGS per SM)
     uint64_t pool_gap = 0;           // unused events between the stimulus and the first gate output (GLS_POOL_GAP_EVENTS)
+    double pool_ratio = 0.0;         // gate-output pool events per (mean stimulus list x input pins) seen so far
     // learned presize (GLS_ALLOC_LEARNED)
     DevBuf feat_static;              // per driver x 32 static features
     DevBuf mlp_params, mlp_img;      // FP32 parameters and the BF16 weight image

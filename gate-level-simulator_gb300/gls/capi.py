@@ -28,7 +28,8 @@ EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "
             "gls_stats_get", "gls_cell_lut", "gls_abi_version", "gls_run_level_static",
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
-            "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched"]
+            "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched",
+            "gls_autotune"]
 
 
 class GlsError(RuntimeError):
@@ -70,6 +71,11 @@ class Stats(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("max_wave", C.c_uint32), ("use_graph", C.c_int), ("saif_only", C.c_int)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("best", C.c_uint32), ("windows", C.c_uint32),
+                ("seg_per_sm", C.c_uint32 * 16), ("warp_mask", C.c_uint32 * 16), ("ms", C.c_float * 16)]
 
 
 class PresizeModel(C.Structure):
@@ -123,6 +129,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_run_level_static.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]
     lib.gls_run_batched.argtypes = [C.c_void_p, C.POINTER(BatchOpts)]
+    lib.gls_autotune.argtypes = [C.c_void_p, C.POINTER(BatchOpts), C.POINTER(TuneResult)]
     lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
     lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -238,6 +245,14 @@ class Simulator:
         """All added windows in waves, each level one launch per kernel over a wave."""
         o = BatchOpts(max_wave, 1 if use_graph else 0, 1 if saif_only else 0)
         self._check(self.lib.gls_run_batched(self.h, C.byref(o)), "run_batched")
+
+    def autotune(self, max_wave: int = 0, use_graph: bool = True, saif_only: bool = False) -> dict:
+        """Time the candidate schedules on the first wave; keep the fastest."""
+        o = BatchOpts(max_wave, 1 if use_graph else 0, 1 if saif_only else 0)
+        r = TuneResult()
+        self._check(self.lib.gls_autotune(self.h, C.byref(o), C.byref(r)), "autotune")
+        cands = [{"seg_per_sm": r.seg_per_sm[k], "warp_mask": r.warp_mask[k], "ms": r.ms[k]} for k in range(r.n)]
+        return {"best": cands[r.best], "windows": r.windows, "candidates": cands}
 
     def saif(self, window: int = 0) -> np.ndarray:
         """(n_nets, 3) uint64: T0, T1, TX; UINT64_MAX rows were not produced."""

@@ -183,6 +183,22 @@ typedef struct {
 } gls_batch_opts;
 int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts);
 
+/* Autotuner: runs the first wave of the added windows (as gls_run_batched
+ * would form it) under every candidate schedule -- time segments per SM for
+ * the thread-per-segment gate kernel (1024, 2048, 4096) times the fan-in
+ * classes that run warp-per-segment (none, 1-input, 1- to 3-input) -- and
+ * keeps the fastest for the context's later runs.  Results never depend on
+ * the schedule. */
+typedef struct {
+    uint32_t n;               /* candidates tried */
+    uint32_t best;            /* index of the one kept */
+    uint32_t windows;         /* windows in the timed wave */
+    uint32_t seg_per_sm[16];
+    uint32_t warp_mask[16];
+    float ms[16];             /* device time of the wave under each */
+} gls_tune_result;
+int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_result *res);
+
 /* T0 / T1 / TX per net for a window (arrays of n_nets).  Nets the run did
  * not produce read UINT64_MAX.  Replaces the SAIF integrals of
  * src/simulate.cu:174-253, 1592-1677 (serial: src/simulate.cpp:102-163). */

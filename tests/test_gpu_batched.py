@@ -116,3 +116,17 @@ def test_batched_random_cases_vs_oracle(gpu, oracle_bin):
             ow, osaif, _ = run_oracle(nl, st, tb, te)
             gw = {n: s.waveform(n, w) for n in ow}
             assert_same(gw, s.saif(w), ow, osaif, f"window {w}")
+
+
+def test_autotune_keeps_results(design, gpu):
+    nl, wins = design
+    ref, _, _ = run_all(nl, wins)
+    with Simulator() as s:
+        s.load(nl)
+        ids = [s.add_window(st, 0, t_end) for st, t_end in wins]
+        t = s.autotune(max_wave=4)
+        assert len(t["candidates"]) == 9 and t["windows"] == 4
+        assert t["best"]["ms"] == min(c["ms"] for c in t["candidates"])
+        s.run_batched(max_wave=4)
+        for w, (la, sa) in zip(ids, ref):
+            assert np.array_equal(s.lengths(w), la) and np.array_equal(s.saif(w), sa)
