@@ -237,7 +237,7 @@ def gls_arm(args):
     sim = Simulator(device=local, stream=stream.cuda_stream, profile=True, seg_events=args.seg, alloc_mode=alloc)
     if args.alloc == "learned":
         from gls import presize
-        sim.set_presize_model(presize.load(args.model or presize.DEFAULT_MODEL))
+        sim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
     sim.load(nl)
     w = sim.add_window(st, 0, cfg.t_end)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
@@ -267,6 +267,17 @@ def gls_arm(args):
         torch.cuda.synchronize()
     barrier()
     step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    presize_q = None
+    if args.alloc == "learned":
+        # the predictor against the lengths this run produced (unseen stimulus seed)
+        from gls import presize
+        params, margin, slack = presize.load(args.model or presize.DEFAULT_MODEL)
+        f, c = sim.presize_samples(w)
+        q = presize.evaluate(sim.presize_predict(params, f), c, margin, slack)
+        presize_q = {"gate_outputs": int(len(c)), "overflows": int(stats["presize_overflows"]),
+                     "overflow_rate": stats["presize_overflows"] / max(1, len(c)), "margin": margin,
+                     "mae_events": q["mae_events"], "mae_log": q["mae_log"],
+                     "reserve_over_exact": q["reserve_over_exact"]}
     if world > 1:
         t = torch.tensor([step_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -338,7 +349,10 @@ def gls_arm(args):
         "gpu_launches": int(stats["launches"]) * args.steps,
         "clocks": clk.summary(),
         "pool_bytes": stats["pool_bytes"],
+        "pool_used_bytes": 4 * stats["pool_used"],
     }
+    if presize_q is not None:
+        line["presize"] = presize_q
     if rank == 0 and not args.no_cpu_baseline:
         sim.add_window(st, 0, cfg.t_end)
         sim.run()
@@ -398,7 +412,7 @@ def batched_arm(args):
     sim = Simulator(alloc_mode=alloc)
     if args.alloc == "learned":
         from gls import presize
-        sim.set_presize_model(presize.load(args.model or presize.DEFAULT_MODEL))
+        sim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
     sim.load(nl)
     for st, t_end in wins:
         sim.add_window(st, 0, t_end)
