@@ -62,6 +62,7 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
     a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
+    a->wave_e = nullptr;
 }
 
 namespace {
@@ -167,10 +168,54 @@ void ctx_drop_graphs(gls_ctx *ctx)
 }
 
 // a window's large device buffers go; its SAIF counts, lengths and flags stay
-static void release_window_pool(Window *w)
+// a window's large device buffers go to the context's spares (saif_only);
+// its SAIF counts, lengths and flags stay
+static void release_window_pool(gls_ctx *ctx, Window *w)
 {
-    w->pool.release(); w->net_off.release(); w->init_off.release(); w->init_len.release(); w->stim_dev.release();
+    DevBuf *bufs[] = {&w->pool, &w->net_off, &w->init_off, &w->init_len, &w->stim_dev};
+    for (DevBuf *b : bufs) {
+        if (b->p) ctx->spare_bufs.push_back(*b);
+        b->p = nullptr;
+        b->bytes = 0;
+    }
     w->uploaded = false;
+}
+
+static void free_spares(gls_ctx *ctx)
+{
+    for (DevBuf &b : ctx->spare_bufs) b.release();
+    ctx->spare_bufs.clear();
+}
+
+static uint64_t spare_bytes(const gls_ctx *ctx)
+{
+    uint64_t t = 0;
+    for (const DevBuf &b : ctx->spare_bufs) t += b.bytes;
+    return t;
+}
+
+// dst holds at least `bytes`: kept if it does, else the smallest spare that
+// does, else a new allocation (spares are freed first if memory is short)
+static cudaError_t take_buf(gls_ctx *ctx, DevBuf &dst, size_t bytes)
+{
+    if (dst.p && dst.bytes >= bytes) return cudaSuccess;
+    size_t best = SIZE_MAX;
+    for (size_t k = 0; k < ctx->spare_bufs.size(); ++k)
+        if (ctx->spare_bufs[k].bytes >= bytes && (best == SIZE_MAX || ctx->spare_bufs[k].bytes < ctx->spare_bufs[best].bytes))
+            best = k;
+    if (best != SIZE_MAX) {
+        if (dst.p) ctx->spare_bufs.push_back(dst);
+        dst = ctx->spare_bufs[best];
+        ctx->spare_bufs.erase(ctx->spare_bufs.begin() + (long)best);
+        return cudaSuccess;
+    }
+    cudaError_t e = dst.ensure(bytes);
+    if (e == cudaErrorMemoryAllocation && !ctx->spare_bufs.empty()) {
+        cudaGetLastError();
+        free_spares(ctx);
+        e = dst.ensure(bytes);
+    }
+    return e;
 }
 
 extern "C" int gls_destroy(gls_ctx *ctx)
@@ -183,6 +228,8 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     ctx_drop_graphs(ctx);
     ctx->hwave.release();
     ctx->dwave.release();
+    ctx->wave_e.release();
+    free_spares(ctx);
     for (LevelScratch *l : ctx->lsc) {
         l->release();
         delete l;
@@ -419,6 +466,7 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
        "upload net delays");
     CK(cudaMemcpy(ctx->lut.p, h_lut.data(), h_lut.size(), cudaMemcpyHostToDevice), "upload lut");
     ctx_drop_graphs(ctx);   // they hold the previous netlist's tables
+    free_spares(ctx);
     ctx->seg_cap = std::max<uint32_t>(1u << 21, 8 * ctx->max_width + 64);
     if (ctx->lsc.empty()) ctx->lsc.push_back(new LevelScratch);
     for (LevelScratch *l : ctx->lsc) l->release();
@@ -447,19 +495,21 @@ static uint64_t projected_cap(const gls_ctx *ctx, const Window *w)
     return cap;
 }
 
-static int upload_window(gls_ctx *ctx, Window *w)
+// Device buffers of a window filled from its host staging.  Without `sync`
+// the copies only precede later work on the context's stream.
+static int upload_window(gls_ctx *ctx, Window *w, bool sync = true)
 {
     const uint64_t n = ctx->n_nets;
-    if (w->pool.bytes < projected_cap(ctx, w) * 4) w->pool.release();
     w->cap = std::max(w->cap, projected_cap(ctx, w));
-    CK(w->pool.ensure(w->cap * 4), "alloc event pool");
-    CK(w->net_off.ensure(n * 8), "alloc net_off");
+    if (w->pool.p && w->pool.bytes < w->cap * 4) w->pool.release();
+    CK(take_buf(ctx, w->pool, w->cap * 4), "alloc event pool");
+    CK(take_buf(ctx, w->net_off, n * 8), "alloc net_off");
     CK(w->net_len.ensure(n * 4), "alloc net_len");
-    CK(w->init_off.ensure(n * 8), "alloc init_off");
-    CK(w->init_len.ensure(n * 4), "alloc init_len");
+    CK(take_buf(ctx, w->init_off, n * 8), "alloc init_off");
+    CK(take_buf(ctx, w->init_len, n * 4), "alloc init_len");
     CK(w->saif.ensure(n * 24), "alloc saif");
     CK(w->small.ensure(256), "alloc counters");
-    CK(w->stim_dev.ensure(w->stim_nets.size() * 4), "alloc stim nets");
+    CK(take_buf(ctx, w->stim_dev, w->stim_nets.size() * 4 + 16), "alloc stim nets");
     if (w->stim_events)
         CK(cudaMemcpyAsync(w->pool.p, w->h_words.p, w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
            "upload stimulus");
@@ -478,7 +528,7 @@ static int upload_window(gls_ctx *ctx, Window *w)
         CK(cudaMemcpyAsync(w->stim_dev.p, w->stim_nets.data(), w->stim_nets.size() * 4, cudaMemcpyHostToDevice,
                            ctx->stream),
            "upload stim nets");
-    CK(cudaStreamSynchronize(ctx->stream), "upload sync");
+    if (sync) CK(cudaStreamSynchronize(ctx->stream), "upload sync");
     w->uploaded = true;
     return GLS_OK;
 }
@@ -673,10 +723,22 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
     if (prof) prof_mark(ctx);
     LevelArgs a;
     ctx_level_args(ctx, &a);
-    for (size_t L = 0; L + 1 < ctx->drv_level_start.size(); ++L) {
+    const size_t nlev = ctx->drv_level_start.size() - 1;
+    if (nwin > 1) {
+        // per level, the wave's fan-in events per class: segments are cut to
+        // one size across the windows of the wave
+        CK(ctx->wave_e.ensure(nlev * kClasses * 8 + 8), "alloc wave totals");
+        CK(cudaMemsetAsync(ctx->wave_e.p, 0, nlev * kClasses * 8, ctx->stream), "clear wave totals");
+    }
+    for (size_t L = 0; L < nlev; ++L) {
         a.lo = ctx->drv_level_start[L];
         a.hi = ctx->drv_level_start[L + 1];
         if (a.hi == a.lo) continue;
+        a.wave_e = nwin > 1 ? ctx->wave_e.as<unsigned long long>() + L * kClasses : nullptr;
+        if (nwin > 1) {
+            launch_wave_events(dw, nwin, a, ctx->stream);
+            ++*launches;
+        }
         if (a.alloc_mode == kAllocLearned) {
             // the level's presize predictions (tensor cores) before its slots are planned
             PresizeArgs pa;
@@ -870,7 +932,7 @@ static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
     cudaSetDevice(ctx->opts.device);
     const size_t nw = ctx->windows.size();
     if (o.saif_only)
-        for (Window *w : ctx->windows) release_window_pool(w);
+        for (Window *w : ctx->windows) release_window_pool(ctx, w);
     // windows per wave: all of them, or with saif_only as many as free device
     // memory holds (each needs its pool, net tables and a level work space)
     uint64_t b = std::min<uint64_t>(std::max<size_t>(nw, 1), kMaxWave);
@@ -878,6 +940,7 @@ static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
     if (o.saif_only) {
         size_t fr = 0, tot = 0;
         cudaMemGetInfo(&fr, &tot);
+        fr += spare_bytes(ctx);
         uint64_t per = 0;
         for (Window *w : ctx->windows) per = std::max<uint64_t>(per, projected_cap(ctx, w) * 4);
         per += (uint64_t)ctx->n_nets * 48 + (uint64_t)(ctx->max_width + 1) * 32 +
@@ -890,6 +953,8 @@ static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
         CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
     if (!ctx->hwave.ensure(kMaxWave * sizeof(WinDev))) return fail(ctx, GLS_ENOMEM, "pinned wave descriptors");
     CK(ctx->dwave.ensure(kMaxWave * sizeof(WinDev)), "alloc wave descriptors");
+    // allocated here, never inside a stream capture
+    CK(ctx->wave_e.ensure((ctx->drv_level_start.size() - 1) * kClasses * 8 + 8), "alloc wave totals");
     *B = b;
     return GLS_OK;
 }
@@ -906,7 +971,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
     for (uint32_t k = 0; k < nwin; ++k) {
         Window *w = ctx->windows[w0 + k];
-        int rc = w->uploaded ? GLS_OK : upload_window(ctx, w);
+        int rc = w->uploaded ? GLS_OK : upload_window(ctx, w, false);
         if (rc == GLS_OK) rc = reset_window(ctx, w);
         if (rc) return rc;
         w->saif_only = false;
@@ -968,7 +1033,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         int rc = settle_window(ctx, w, acc);
         if (rc) return rc;
         if (o.saif_only) {
-            release_window_pool(w);
+            release_window_pool(ctx, w);
             w->saif_only = true;
         }
     }
@@ -979,7 +1044,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         int rc = settle_window(ctx, w, acc);
         if (rc) return rc;
         if (o.saif_only) {
-            release_window_pool(w);
+            release_window_pool(ctx, w);
             w->saif_only = true;
         }
     }
@@ -1005,6 +1070,7 @@ extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
             // pools grow with what earlier windows needed: refit the wave to free memory
             size_t fr = 0, tot = 0;
             cudaMemGetInfo(&fr, &tot);
+            fr += spare_bytes(ctx);
             uint64_t per = 1;
             for (uint64_t k = 0; k < nwin; ++k) {
                 const Window *w = ctx->windows[w0 + k];

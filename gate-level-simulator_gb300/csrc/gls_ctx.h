@@ -155,6 +155,8 @@ struct gls_ctx {
     // the captured launch graphs, one per wave shape
     PinBuf hwave;
     DevBuf dwave;
+    DevBuf wave_e;                   // per level: a wave's fan-in events per class
+    std::vector<DevBuf> spare_bufs;  // device buffers of windows that ran saif_only, reused by later windows
     struct WaveGraph {
         uint64_t key;
         cudaGraphExec_t exec;

@@ -150,6 +150,7 @@ struct LevelArgs {
     uint32_t warp_mask;         // bit c: fan-in class c runs the warp-per-segment kernel
     uint32_t def_delay;         // delay used when no arc applies
     uint32_t alloc_mode;        // kAllocBound / kAllocExact / kAllocLearned
+    unsigned long long *wave_e; // wave of windows: fan-in events of the level per class over all windows (else null)
 };
 
 // Windows simulated together: every level kernel takes a device array of
@@ -163,6 +164,9 @@ __host__ __device__ inline int fanin_class(int m) { return m <= 1 ? 0 : (m == 2 
 // (used when nwin == 1), `dw` the device array of all nwin descriptors.
 void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, cudaStream_t st);
 void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
+// a wave's fan-in events per class into a.wave_e (cleared before), so every
+// window of the wave cuts its segments to the same size
+void launch_wave_events(const WinDev *dw, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
 void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,
                 int sm_count, cudaStream_t st);
 void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st);

@@ -152,6 +152,32 @@ __device__ T block_excl_scan(T x, T *total, T *sm)
     return pre + inc - x;
 }
 
+// One block per window of a wave: the level's fan-in events per fan-in class,
+// summed over the wave into a.wave_e.
+__global__ void __launch_bounds__(1024) k_wave_events(const WinDev *__restrict__ wv, LevelArgs a)
+{
+    __shared__ unsigned long long sm64[32];
+    const WinDev &w = wv[blockIdx.x];
+    const uint32_t n = a.hi - a.lo;
+    unsigned long long e_cls[kClasses] = {0, 0, 0, 0};
+    if (!*w.err) {
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const DrvMeta &md = a.meta[a.lo + i];
+            unsigned long long E = 0;
+            for (int j = 0; j < md.m; ++j) E += w.net_len[md.net[j]];
+            const int c = fanin_class(md.m);
+#pragma unroll
+            for (int k = 0; k < kClasses; ++k) if (k == c) e_cls[k] += E;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kClasses; ++k) {
+        unsigned long long tot;
+        block_excl_scan<unsigned long long>(e_cls[k], &tot, sm64);
+        if (threadIdx.x == 0 && tot) atomicAdd(&a.wave_e[k], tot);
+    }
+}
+
 // The windows a launch covers: one window passed by value (kernel
 // parameter space, no indirection in the hot loops), or a device array.
 template <bool kBatch> struct WinSet;
@@ -217,7 +243,8 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             unsigned long long seg = a.seg_events;
             const bool warp = (a.warp_mask >> k) & 1u;
             const unsigned long long target = warp ? a.seg_target_w : a.seg_target;
-            if (!seg) seg = max(warp ? 128ull : 32ull, (e_cls[k] + target - 1) / max(1ull, target));
+            const unsigned long long ev = a.wave_e ? a.wave_e[k] : e_cls[k];   // the wave shares the GPU
+            if (!seg) seg = max(warp ? 128ull : 32ull, (ev + target - 1) / max(1ull, target));
             s_seg[k] = (uint32_t)min(max(seg, floor_seg), 0x7FFFFFFFull);
         }
         s_base = *w.top;
@@ -1322,6 +1349,11 @@ void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t
     if (!max_stim || !nwin) return;
     const dim3 grid((uint32_t)(((uint64_t)max_stim * 32 + 255) / 256), nwin);
     GLS_DISPATCH(h, dw, nwin, (k_stim_saif<<<grid, 256, 0, st>>>(ws)));
+}
+
+void launch_wave_events(const WinDev *dw, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
+{
+    k_wave_events<<<nwin, 1024, 0, st>>>(dw, a);
 }
 
 void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
