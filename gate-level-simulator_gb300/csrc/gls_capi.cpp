@@ -52,6 +52,7 @@ int ctx_fail(gls_ctx *c, int code, const char *fmt, ...)
 void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
 {
     a->meta = ctx->meta.as<DrvMeta>();
+    a->slut = ctx->slut.as<uint4>();
     a->arcs = ctx->arcs.as<ArcDev>();
     a->ndel = ctx->ndel.as<NetDelay>();
     a->lut = ctx->lut.as<uint8_t>();
@@ -117,6 +118,11 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
             ctx->own_stream = true;
         }
     }
+    for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
+        e = cudaStreamCreateWithFlags(&ctx->side[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e != cudaSuccess) {
@@ -128,6 +134,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
     // 2: three) run warp-per-segment, and how many segments per SM those
     // classes are cut into
     if (const char *v = getenv("GLS_SIM_WARP_MASK")) ctx->warp_mask = (uint32_t)strtoul(v, nullptr, 0) & 7u;
+    if (const char *v = getenv("GLS_SIM_CONCURRENT")) ctx->concurrent = strtoul(v, nullptr, 0) != 0;
     uint32_t per_sm = 128;
     if (const char *v = getenv("GLS_SIM_WARP_SEGS")) per_sm = std::max(1u, (uint32_t)strtoul(v, nullptr, 0));
     ctx->seg_target_w = (uint32_t)ctx->sm_count * per_sm;
@@ -224,7 +231,7 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     gls_clear_windows(ctx);
     for (Window *w : ctx->spare) free_window(w);
     ctx->spare.clear();
-    ctx->meta.release(); ctx->arcs.release(); ctx->ndel.release(); ctx->lut.release();
+    ctx->meta.release(); ctx->arcs.release(); ctx->ndel.release(); ctx->lut.release(); ctx->slut.release();
     ctx_drop_graphs(ctx);
     ctx->hwave.release();
     ctx->dwave.release();
@@ -240,6 +247,11 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    for (int c = 0; c < kClasses; ++c) {
+        if (ctx->side[c]) cudaStreamDestroy(ctx->side[c]);
+        if (ctx->join_ev[c]) cudaEventDestroy(ctx->join_ev[c]);
+    }
+    if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     delete ctx;
     return GLS_OK;
 }
@@ -453,6 +465,25 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
         f[30] = (md.flags & kFlagRegular) ? 1.f : 0.f;
         f[31] = 1.f;
     }
+    // per gate output with at most 3 input nets: its truth table indexed by
+    // the input nets' values (what the gate kernels keep in registers)
+    std::vector<uint4> h_slut(h_meta.size(), make_uint4(0, 0, 0, 0));
+    for (size_t d = 0; d < ctx->n_drv; ++d) {
+        const DrvMeta &md = h_meta[d];
+        if (md.m > 3) continue;
+        uint32_t words[4] = {0, 0, 0, 0};
+        const uint32_t entries = 1u << (2 * std::max<int>(md.m, 1));
+        for (uint32_t x = 0; x < entries; ++x) {
+            uint32_t idx = 0;
+            for (int p = 0; p < md.n_pins; ++p)
+                idx |= ((x >> (2 * ((md.pin_slot >> (3 * p)) & 7u))) & 3u) << (2 * p);
+            words[x >> 4] |= (uint32_t)(h_lut[md.lut_off + idx] & 3u) << (2 * (x & 15u));
+        }
+        h_slut[d] = make_uint4(words[0], words[1], words[2], words[3]);
+    }
+    CK(ctx->slut.ensure(h_slut.size() * sizeof(uint4)), "alloc slot truth tables");
+    CK(cudaMemcpy(ctx->slut.p, h_slut.data(), h_slut.size() * sizeof(uint4), cudaMemcpyHostToDevice),
+       "upload slot truth tables");
     CK(ctx->feat_static.ensure(h_feat.size() * 4), "alloc presize features");
     CK(cudaMemcpy(ctx->feat_static.p, h_feat.data(), h_feat.size() * 4, cudaMemcpyHostToDevice),
        "upload presize features");
@@ -752,12 +783,28 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
         }
         launch_plan(dw, h0, nwin, a, ctx->stream);
         if (prof) prof_mark(ctx);
+        int n_cls = 0;
+        for (int c = 0; c < kClasses; ++c)
+            n_cls += ctx->cls_start[(kClasses + 1) * L + c + 1] > ctx->cls_start[(kClasses + 1) * L + c];
+        const bool fork = ctx->concurrent && n_cls > 1;
+        if (fork) CK(cudaEventRecord(ctx->fork_ev, ctx->stream), "fork");
+        bool first = true;
         for (int c = 0; c < kClasses; ++c) {
             const uint32_t d0 = ctx->cls_start[(kClasses + 1) * L + c], d1 = ctx->cls_start[(kClasses + 1) * L + c + 1];
-            if (d1 > d0) {
-                launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, ctx->stream);
-                ++*launches;
+            if (d1 <= d0) continue;
+            // the first class on the main stream, the others beside it
+            cudaStream_t st = ctx->stream;
+            if (fork && !first) {
+                st = ctx->side[c];
+                CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
             }
+            launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, st);
+            if (st != ctx->stream) {
+                CK(cudaEventRecord(ctx->join_ev[c], st), "join");
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[c], 0), "join wait");
+            }
+            first = false;
+            ++*launches;
         }
         if (prof) prof_mark(ctx);
         launch_link(dw, h0, nwin, a, ctx->stream);

@@ -117,6 +117,11 @@ struct gls_ctx {
     gls_opts opts{};
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // fan-in classes of a level run concurrently: side streams fork after the
+    // plan and join before the link (GLS_SIM_CONCURRENT=0 runs them in turn)
+    cudaStream_t side[gls::kClasses] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[gls::kClasses] = {};
+    bool concurrent = true;
     int sm_count = 0;
     std::string err;
     bool loaded = false;
@@ -128,7 +133,7 @@ struct gls_ctx {
     uint64_t pins_total = 0;
     std::vector<uint8_t> driven;             // net driven by a gate output
     std::vector<uint32_t> ext_inputs;        // nets read by gates and driven by no gate
-    DevBuf meta, arcs, ndel, lut;
+    DevBuf meta, arcs, ndel, lut, slut;
     std::vector<LevelScratch *> lsc;         // level work spaces ([0]: sequential runs)
     uint32_t seg_cap = 0;                    // segment-table size new work spaces get
     uint64_t scr_cap = 0;                    // stack words new work spaces get

@@ -140,6 +140,8 @@ static_assert(sizeof(WinDev) <= 192, "WinDev fits the static entry point's descr
 
 struct LevelArgs {
     const DrvMeta *meta;
+    const uint4 *slut;          // per driver with at most 3 input nets: truth table over its input nets' values,
+                                // 2 bits per entry, entry = sum(value(net j) << 2j) (64 entries in 128 bits)
     const ArcDev *arcs;
     const NetDelay *ndel;
     const uint8_t *lut;

@@ -390,10 +390,29 @@ struct Reader {
     }
 };
 
+// x * y / z for 32-bit operands, in 32-bit arithmetic when the product fits
+__device__ __forceinline__ uint32_t mul_div(uint32_t x, uint32_t y, uint32_t z)
+{
+    if (__umulhi(x, y) == 0) return (x * y) / z;
+    return (uint32_t)((uint64_t)x * y / z);
+}
+
+// output value for the input-net values `curp` (2 bits per net) from the
+// slot truth table held in registers
+template <int M>
+__device__ __forceinline__ uint32_t slut_get(const uint4 &t, uint32_t curp)
+{
+    const uint32_t x = curp & ((1u << (2 * M)) - 1u);
+    uint32_t wd = t.x;
+    if (M == 3) wd = (x >> 4) == 0 ? t.x : ((x >> 4) == 1 ? t.y : ((x >> 4) == 2 ? t.z : t.w));
+    return (wd >> (2 * (x & 15u))) & 3u;
+}
+
 template <int M>
 __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t s,
-                            uint32_t S, uint32_t seg_id, uint64_t scr)
+                            uint32_t S, uint32_t seg_id, uint64_t scr, const uint4 sl)
 {
+    constexpr bool kSlut = M <= 3;   // truth table in registers
     const uint4 *P = reinterpret_cast<const uint4 *>(w.pool);
     uint64_t off[M];
     uint32_t len[M];
@@ -413,7 +432,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
 #pragma unroll
     for (int j = 0; j < M; ++j) if (j == piv) poff = off[j];
     const uint32_t *pt = w.pool + poff;
-    const uint32_t plo = (uint32_t)((uint64_t)s * plen / S), phi = (uint32_t)((uint64_t)(s + 1) * plen / S);
+    const uint32_t plo = mul_div(s, plen, S), phi = mul_div(s + 1, plen, S);
     const uint32_t tlo = s > 0 ? ev_time(pt[plo]) : 0u;
     const uint32_t thi = s + 1 < S ? ev_time(pt[phi]) : kInf;
     uint32_t curp = 0x555u;   // every slot X
@@ -425,8 +444,8 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     for (int j = 0; j < M; ++j) {
         uint32_t b = 0, e = 0;
         if (j < md.m) {
-            const uint32_t gl = plen ? (uint32_t)((uint64_t)plo * len[j] / plen) : 0u;
-            const uint32_t gh = plen ? (uint32_t)((uint64_t)phi * len[j] / plen) : 0u;
+            const uint32_t gl = plen ? mul_div(plo, len[j], plen) : 0u;
+            const uint32_t gh = plen ? mul_div(phi, len[j], plen) : 0u;
             b = s > 0 ? (j == piv ? plo : search_from(w.pool + off[j], len[j], tlo, gl)) : 0u;
             e = s + 1 < S ? (j == piv ? phi : search_from(w.pool + off[j], len[j], thi, gh)) : len[j];
             region += b;
@@ -446,7 +465,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     uint32_t cnt = 0, top = 0;        // stack size and its top word
     int popped_v = -1;
     if (s == 0) { top = ev_word(0, kVX); ot[0] = top; cnt = 1; }
-    uint32_t fprev = before ? lut[lut_index(curp, md)] : kVX;
+    uint32_t fprev = before ? (kSlut ? slut_get<M>(sl, curp) : lut[lut_index(curp, md)]) : kVX;
     uint32_t min_o = kInf;
     for (;;) {
         uint32_t mk = hk[0] | 3u;
@@ -464,7 +483,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
                 hk[j] = rd[j].head();
             }
         }
-        const uint32_t F = lut[lut_index(curp, md)];
+        const uint32_t F = kSlut ? slut_get<M>(sl, curp) : lut[lut_index(curp, md)];
         if (F == fprev) continue;
         const int so = (int)((kSenseTab >> (3 * (fprev * 4 + F))) & 7u);
         fprev = F;
@@ -562,7 +581,8 @@ __global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4))
     }
     const uint32_t per = (total + gridDim.x - 1) / gridDim.x;
     const uint32_t b0 = g0 + min(total, blockIdx.x * per), b1 = g0 + min(total, (blockIdx.x + 1) * per);
-    if (threadIdx.x == 0) s_next = b0;
+    __shared__ uint32_t s_hint;   // a driver near the block's latest segment
+    if (threadIdx.x == 0) { s_next = b0; s_hint = d0; }
     __syncthreads();
     for (;;) {
         const uint32_t q = atomicAdd(&s_next, 1u);
@@ -570,17 +590,35 @@ __global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? 6 : 4))
         const uint32_t win = kBatch ? window_of(s_pre, nwin, q) : 0u;
         const WinDev &w = ws.get(win);
         const uint32_t g = kBatch ? q - s_pre[win] + w.seg_base[d0] : q;
-        // driver owning segment g: last i in [d0, d1) with seg_base[i] <= g
+        // driver owning segment g: last i in [d0, d1) with seg_base[i] <= g.
+        // Segments go out in increasing order, so with one window the block's
+        // latest driver is a close guess: gallop from it, then bisect.
         uint32_t lo = d0, hi = d1;
+        if (!kBatch) {
+            const uint32_t h = min(max(*(volatile uint32_t *)&s_hint, d0), d1 - 1);
+            if (w.seg_base[h] <= g) {
+                lo = h;
+                uint32_t step = 1;
+                while (lo + step < d1 && w.seg_base[lo + step] <= g) { lo += step; step <<= 1; }
+                hi = min(d1, lo + step);
+            } else {
+                hi = h;
+                uint32_t step = 1;
+                while (hi - d0 > step && w.seg_base[hi - step] > g) { hi -= step; step <<= 1; }
+                lo = hi - d0 > step ? hi - step : d0;
+            }
+        }
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (w.seg_base[mid] <= g) lo = mid; else hi = mid;
         }
         const uint32_t i = lo;
+        if (!kBatch) s_hint = i;
         const uint32_t sb = w.seg_base[i];
         const uint32_t S = w.seg_base[i + 1] - sb;
         const DrvMeta md = a.meta[a.lo + i];
-        sim_segment<M>(w, a, md, g - sb, S, g, w.scr[i]);
+        const uint4 sl = M <= 3 ? __ldg(a.slut + a.lo + i) : make_uint4(0, 0, 0, 0);
+        sim_segment<M>(w, a, md, g - sb, S, g, w.scr[i], sl);
     }
 }
 
