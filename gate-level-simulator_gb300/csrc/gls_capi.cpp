@@ -63,6 +63,7 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->warp_mask = ctx->warp_mask;
     a->def_delay = ctx->def_delay;
     a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
+    a->copy_lanes = ctx->copy_lanes;
     a->wave_e = nullptr;
 }
 
@@ -135,6 +136,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
     // classes are cut into
     if (const char *v = getenv("GLS_SIM_WARP_MASK")) ctx->warp_mask = (uint32_t)strtoul(v, nullptr, 0) & 7u;
     if (const char *v = getenv("GLS_SIM_CONCURRENT")) ctx->concurrent = strtoul(v, nullptr, 0) != 0;
+    if (const char *v = getenv("GLS_COPY_LANES")) ctx->copy_lanes = (uint32_t)strtoul(v, nullptr, 0);
     uint32_t per_sm = 128;
     if (const char *v = getenv("GLS_SIM_WARP_SEGS")) per_sm = std::max(1u, (uint32_t)strtoul(v, nullptr, 0));
     ctx->seg_target_w = (uint32_t)ctx->sm_count * per_sm;

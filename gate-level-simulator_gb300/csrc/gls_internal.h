@@ -152,6 +152,7 @@ struct LevelArgs {
     uint32_t warp_mask;         // bit c: fan-in class c runs the warp-per-segment kernel
     uint32_t def_delay;         // delay used when no arc applies
     uint32_t alloc_mode;        // kAllocBound / kAllocExact / kAllocLearned
+    uint32_t copy_lanes;        // lanes per segment in the copy kernel (4, 8, 16 or 32)
     unsigned long long *wave_e; // wave of windows: fan-in events of the level per class over all windows (else null)
 };
 

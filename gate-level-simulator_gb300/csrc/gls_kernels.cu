@@ -182,11 +182,13 @@ __global__ void __launch_bounds__(1024) k_wave_events(const WinDev *__restrict__
 // parameter space, no indirection in the hot loops), or a device array.
 template <bool kBatch> struct WinSet;
 template <> struct WinSet<false> {
+    static constexpr bool kIsBatch = false;
     WinDev w;
     __device__ __forceinline__ const WinDev &get(uint32_t) const { return w; }
     __device__ __forceinline__ uint32_t size() const { return 1; }
 };
 template <> struct WinSet<true> {
+    static constexpr bool kIsBatch = true;
     const WinDev *wv;
     uint32_t n;
     __device__ __forceinline__ const WinDev &get(uint32_t k) const { return wv[k]; }
@@ -1267,14 +1269,13 @@ __device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, 
     if (any) { cprev = cn; pclass = pn; }
 }
 
-// k_copy: one 16-lane group per segment: copy the kept entries from the
+// k_copy: one W-lane group per segment: copy the kept entries from the
 // level scratch into the pool and add their SAIF contributions to the gate
 // output's counters.  The next segment's record is loaded while the current
 // one is copied.
-template <bool kBatch>
+template <bool kBatch, int W>
 __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs a)
 {
-    constexpr int W = 16;
     const unsigned FULL = 0xffffffffu;
     __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
     __shared__ uint32_t sm32[32];
@@ -1437,7 +1438,10 @@ void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
 
 void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st)
 {
-    GLS_DISPATCH(h, dw, nwin, (k_copy<<<sm_count * 8, 256, 0, st>>>(ws, a)));
+    if (a.copy_lanes == 4) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 4><<<sm_count * 8, 256, 0, st>>>(ws, a)));
+    else if (a.copy_lanes == 8) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 8><<<sm_count * 8, 256, 0, st>>>(ws, a)));
+    else if (a.copy_lanes == 32) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 32><<<sm_count * 8, 256, 0, st>>>(ws, a)));
+    else GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 16><<<sm_count * 8, 256, 0, st>>>(ws, a)));
 }
 
 }  // namespace gls
