@@ -40,7 +40,8 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 
 
 def _compile(src: Path, obj: Path):
-    cmd = [nvcc(), *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]
+    extra = os.environ.get("GLS_NVCC_FLAGS", "").split()   # tuning builds, e.g. -DGLS_SIM3_BLOCKS=7
+    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
