@@ -788,7 +788,11 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
         int n_cls = 0;
         for (int c = 0; c < kClasses; ++c)
             n_cls += ctx->cls_start[(kClasses + 1) * L + c + 1] > ctx->cls_start[(kClasses + 1) * L + c];
-        const bool fork = ctx->concurrent && n_cls > 1;
+        // Concurrent: the fan-in classes simulate on their own streams, so
+        // one class's blocks fill another's tail (linking and copying every
+        // class together after the join measured faster than per class).
+        // Profiled runs keep the classes apart.
+        const bool fork = ctx->concurrent && !(prof && ctx->opts.profile) && n_cls > 1;
         if (fork) CK(cudaEventRecord(ctx->fork_ev, ctx->stream), "fork");
         bool first = true;
         for (int c = 0; c < kClasses; ++c) {
@@ -801,18 +805,19 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
                 CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
             }
             launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, st);
+            ++*launches;
             if (st != ctx->stream) {
                 CK(cudaEventRecord(ctx->join_ev[c], st), "join");
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[c], 0), "join wait");
             }
             first = false;
-            ++*launches;
         }
         if (prof) prof_mark(ctx);
-        launch_link(dw, h0, nwin, a, ctx->stream);
+        launch_link(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->stream);
         launch_copy(dw, h0, nwin, a, ctx->sm_count, ctx->stream);
+        *launches += 2;
         if (prof) prof_mark(ctx);
-        *launches += 3;
+        ++*launches;   // the plan
     }
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;

@@ -1129,13 +1129,14 @@ __device__ __forceinline__ void saif_add(unsigned long long acc[3], int cls, uns
 // before it, places the segments back to back in the gate's pool slot and
 // hands each segment's copy to k_copy with the final event that precedes it.
 template <bool kBatch>
-__global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs a)
+__global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
-    const uint32_t n = a.hi - a.lo;
+    // gate outputs [d0, d1) of the level (one fan-in class, or all)
+    const uint32_t n = d1 - d0;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (gw >= (uint64_t)n * ws.size()) return;
-    const uint32_t i = (uint32_t)(gw % n);
+    const uint32_t i = d0 + (uint32_t)(gw % n);
     const WinDev &w = ws.get((uint32_t)(gw / n));
     if (*w.err) return;
     const unsigned FULL = 0xffffffffu;
@@ -1432,11 +1433,13 @@ void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArg
     GLS_DISPATCH(h, dw, nwin, sim_kernels(ws, a, cls, d0, d1, sm_count, st));
 }
 
-void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
+void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
+                 cudaStream_t st)
 {
-    const uint64_t warps = (uint64_t)(a.hi - a.lo) * nwin;
+    const uint64_t warps = (uint64_t)(d1 - d0) * nwin;
+    if (!warps) return;
     const uint32_t blocks = (uint32_t)((warps * 32 + 255) / 256);
-    GLS_DISPATCH(h, dw, nwin, (k_link<<<blocks, 256, 0, st>>>(ws, a)));
+    GLS_DISPATCH(h, dw, nwin, (k_link<<<blocks, 256, 0, st>>>(ws, a, d0, d1)));
 }
 
 void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st)

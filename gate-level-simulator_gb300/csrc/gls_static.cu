@@ -146,7 +146,7 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
         const uint32_t d0 = std::max(c0, first), d1 = std::min(c1, first + count);
         if (d1 > d0) launch_sim(dw, d, 1, a, c, d0 - first, d1 - first, ctx->sm_count, ctx->stream);
     }
-    launch_link(dw, d, 1, a, ctx->stream);
+    launch_link(dw, d, 1, a, 0, count, ctx->stream);
     launch_copy(dw, d, 1, a, ctx->sm_count, ctx->stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "level kernel launch: %s", cudaGetErrorString(e));

@@ -80,7 +80,8 @@ typedef struct {
     uint32_t seg_events;   /* fan-in events per time segment (0 = default) */
     uint64_t pool_events;  /* initial event-pool capacity (0 = automatic) */
     void *stream;          /* cudaStream_t to launch on (NULL = own stream) */
-    int profile;           /* 1: time every kernel class with CUDA events */
+    int profile;           /* 1: time every kernel class with CUDA events (the fan-in
+                              classes of a level then run one after another) */
 } gls_opts;
 
 /* One library cell: its primitive program in the reference encoding
