@@ -136,6 +136,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
     // classes are cut into
     if (const char *v = getenv("GLS_SIM_WARP_MASK")) ctx->warp_mask = (uint32_t)strtoul(v, nullptr, 0) & 7u;
     if (const char *v = getenv("GLS_SIM_CONCURRENT")) ctx->concurrent = strtoul(v, nullptr, 0) != 0;
+    if (const char *v = getenv("GLS_SIM_PIPELINE")) ctx->pipeline = strtoul(v, nullptr, 0) != 0;
     if (const char *v = getenv("GLS_COPY_LANES")) ctx->copy_lanes = (uint32_t)strtoul(v, nullptr, 0);
     uint32_t per_sm = 128;
     if (const char *v = getenv("GLS_SIM_WARP_SEGS")) per_sm = std::max(1u, (uint32_t)strtoul(v, nullptr, 0));
@@ -806,6 +807,11 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
             }
             launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, st);
             ++*launches;
+            if (fork && ctx->pipeline) {   // the class's link and copy right behind it
+                launch_link(dw, h0, nwin, a, d0, d1, st);
+                launch_copy(dw, h0, nwin, a, d0, d1, ctx->sm_count, st);
+                *launches += 2;
+            }
             if (st != ctx->stream) {
                 CK(cudaEventRecord(ctx->join_ev[c], st), "join");
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[c], 0), "join wait");
@@ -813,9 +819,11 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
             first = false;
         }
         if (prof) prof_mark(ctx);
-        launch_link(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->stream);
-        launch_copy(dw, h0, nwin, a, ctx->sm_count, ctx->stream);
-        *launches += 2;
+        if (!(fork && ctx->pipeline)) {
+            launch_link(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->stream);
+            launch_copy(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->sm_count, ctx->stream);
+            *launches += 2;
+        }
         if (prof) prof_mark(ctx);
         ++*launches;   // the plan
     }

@@ -122,6 +122,7 @@ struct gls_ctx {
     cudaStream_t side[gls::kClasses] = {};
     cudaEvent_t fork_ev = nullptr, join_ev[gls::kClasses] = {};
     bool concurrent = true;
+    bool pipeline = true;            // with concurrent classes: each class links and copies on its own stream
     uint32_t copy_lanes = 8;         // lanes per segment of the copy kernel (GLS_COPY_LANES: 4, 8, 16, 32)
     int sm_count = 0;
     std::string err;

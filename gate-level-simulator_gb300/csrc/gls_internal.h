@@ -172,9 +172,10 @@ void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
 void launch_wave_events(const WinDev *dw, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
 void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,
                 int sm_count, cudaStream_t st);
-// link the gate outputs [d0, d1) of the level (level-relative); copy all of the level's segments
+// link and copy the gate outputs [d0, d1) of the level (level-relative)
 void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
                  cudaStream_t st);
-void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st);
+void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
+                 int sm_count, cudaStream_t st);
 
 }  // namespace gls

@@ -1278,14 +1278,34 @@ __device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, 
 // output's counters.  The next segment's record is loaded while the current
 // one is copied.
 template <bool kBatch, int W>
-__global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs a)
+__global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     const unsigned FULL = 0xffffffffu;
     __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
     __shared__ uint32_t sm32[32];
+    __shared__ uint32_t s_skip, s_base;
     const uint32_t nwin = ws.size();
-    // no flag changes during this kernel: windows that failed are left out
-    const uint32_t nseg = window_prefix<true>(ws, [](const WinDev &x) { return *x.n_segs; }, s_pre, sm32);
+    // The segments of gate outputs [d0, d1), counted from the segment tables
+    // (fixed once planned; a failed plan leaves them zero).  A gate kernel of
+    // another fan-in class may raise a window's flag while this runs: a
+    // window whose flag was up before its link ran is skipped (its copy
+    // records are stale), one raised later is copied harmlessly.
+    uint32_t nseg;
+    if (!kBatch) {
+        if (threadIdx.x == 0) {
+            const WinDev &w = ws.get(0);
+            s_skip = *(volatile uint32_t *)w.err != 0;
+            s_base = w.seg_base[d0];
+            s_pre[0] = 0;
+            s_pre[1] = w.seg_base[d1] - s_base;
+        }
+        __syncthreads();
+        if (s_skip) return;
+        nseg = s_pre[1];
+    } else {
+        nseg = window_prefix<false>(
+            ws, [&](const WinDev &x) { return x.seg_base[d1] - x.seg_base[d0]; }, s_pre, sm32);
+    }
     const int sub = threadIdx.x & (W - 1);
     const uint32_t gpb = blockDim.x / W;
     const uint32_t stride = gridDim.x * gpb;
@@ -1298,7 +1318,9 @@ __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs
         win = 0;
         if (q < nseg) {
             win = window_of(s_pre, nwin, q);
-            c = ws.get(win).copies[q - s_pre[win]];
+            const WinDev &x = ws.get(win);
+            if (!kBatch) c = x.copies[q + s_base];
+            else if (!*(volatile uint32_t *)x.err) c = x.copies[q - s_pre[win] + x.seg_base[d0]];
         }
         return c;
     };
@@ -1442,12 +1464,13 @@ void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
     GLS_DISPATCH(h, dw, nwin, (k_link<<<blocks, 256, 0, st>>>(ws, a, d0, d1)));
 }
 
-void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int sm_count, cudaStream_t st)
+void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
+                 int sm_count, cudaStream_t st)
 {
-    if (a.copy_lanes == 4) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 4><<<sm_count * 8, 256, 0, st>>>(ws, a)));
-    else if (a.copy_lanes == 8) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 8><<<sm_count * 8, 256, 0, st>>>(ws, a)));
-    else if (a.copy_lanes == 32) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 32><<<sm_count * 8, 256, 0, st>>>(ws, a)));
-    else GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 16><<<sm_count * 8, 256, 0, st>>>(ws, a)));
+    if (a.copy_lanes == 4) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 4><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
+    else if (a.copy_lanes == 8) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 8><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
+    else if (a.copy_lanes == 32) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 32><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
+    else GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 16><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
 }
 
 }  // namespace gls

@@ -147,7 +147,7 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
         if (d1 > d0) launch_sim(dw, d, 1, a, c, d0 - first, d1 - first, ctx->sm_count, ctx->stream);
     }
     launch_link(dw, d, 1, a, 0, count, ctx->stream);
-    launch_copy(dw, d, 1, a, ctx->sm_count, ctx->stream);
+    launch_copy(dw, d, 1, a, 0, count, ctx->sm_count, ctx->stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "level kernel launch: %s", cudaGetErrorString(e));
     unsigned long long st[8];
