@@ -246,6 +246,8 @@ def gls_arm(args):
         if world > 1:
             torch.distributed.barrier()
 
+    tune = sim.autotune()   # untimed: the schedule for this workload (results never depend on it)
+    log(f"autotune: {tune['best']}")
     for _ in range(args.warmup):
         sim.run()
     stats = sim.stats()
@@ -336,6 +338,7 @@ def gls_arm(args):
         from gls import presize
         psim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
     psim.load(nl)
+    psim.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"])
     psim.add_window(st, 0, cfg.t_end)
     psim.run()
     for _ in range(args.steps):
@@ -365,7 +368,8 @@ def gls_arm(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
-                   "seg_events": args.seg or "auto", "alloc": args.alloc},
+                   "seg_events": args.seg or "auto", "alloc": args.alloc,
+                   "schedule": {k: tune["best"][k] for k in ("seg_per_sm", "warp_mask")}},
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -1152,6 +1152,17 @@ extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
     return GLS_OK;
 }
 
+extern "C" int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask)
+{
+    if (!ctx) return GLS_EINVAL;
+    if (seg_per_sm < 64 || seg_per_sm > 65536 || warp_mask > 7)
+        return fail(ctx, GLS_EINVAL, "schedule out of range: %u segments per SM, warp mask %u", seg_per_sm, warp_mask);
+    ctx->seg_per_sm = seg_per_sm;
+    ctx->warp_mask = warp_mask;
+    ctx_drop_graphs(ctx);
+    return GLS_OK;
+}
+
 extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_result *res)
 {
     if (!ctx) return GLS_EINVAL;

@@ -29,7 +29,7 @@ EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
             "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched",
-            "gls_autotune"]
+            "gls_autotune", "gls_set_schedule"]
 
 
 class GlsError(RuntimeError):
@@ -130,6 +130,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]
     lib.gls_run_batched.argtypes = [C.c_void_p, C.POINTER(BatchOpts)]
     lib.gls_autotune.argtypes = [C.c_void_p, C.POINTER(BatchOpts), C.POINTER(TuneResult)]
+    lib.gls_set_schedule.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
     lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
     lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -253,6 +254,9 @@ class Simulator:
         self._check(self.lib.gls_autotune(self.h, C.byref(o), C.byref(r)), "autotune")
         cands = [{"seg_per_sm": r.seg_per_sm[k], "warp_mask": r.warp_mask[k], "ms": r.ms[k]} for k in range(r.n)]
         return {"best": cands[r.best], "windows": r.windows, "candidates": cands}
+
+    def set_schedule(self, seg_per_sm: int, warp_mask: int):
+        self._check(self.lib.gls_set_schedule(self.h, seg_per_sm, warp_mask), "set_schedule")
 
     def saif(self, window: int = 0) -> np.ndarray:
         """(n_nets, 3) uint64: T0, T1, TX; UINT64_MAX rows were not produced."""

@@ -199,6 +199,11 @@ typedef struct {
     float ms[16];             /* device time of the wave under each */
 } gls_tune_result;
 int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_result *res);
+/* Set the schedule by hand (e.g. one gls_autotune found for another context
+ * on the same netlist): time segments per SM for the thread-per-segment gate
+ * kernel (64..65536), and which fan-in classes run warp-per-segment (bits
+ * 0-2 for 1-, 2- and 3-input gates). */
+int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask);
 
 /* T0 / T1 / TX per net for a window (arrays of n_nets).  Nets the run did
  * not produce read UINT64_MAX.  Replaces the SAIF integrals of
