@@ -247,7 +247,8 @@ def gls_arm(args):
             torch.distributed.barrier()
 
     tune = sim.autotune()   # untimed: the schedule for this workload (results never depend on it)
-    log(f"autotune: {tune['best']}")
+    log(f"autotune: {tune['best']}; candidates (segments/SM, warp mask, flags: ms): " +
+        ", ".join(f"{c['seg_per_sm']}/{c['warp_mask']}/{c['flags']}: {c['ms']:.2f}" for c in tune["candidates"]))
     for _ in range(args.warmup):
         sim.run()
     stats = sim.stats()
@@ -338,7 +339,7 @@ def gls_arm(args):
         from gls import presize
         psim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
     psim.load(nl)
-    psim.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"])
+    psim.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"], tune["best"]["flags"])
     psim.add_window(st, 0, cfg.t_end)
     psim.run()
     for _ in range(args.steps):
@@ -369,7 +370,7 @@ def gls_arm(args):
         "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
                    "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
                    "seg_events": args.seg or "auto", "alloc": args.alloc,
-                   "schedule": {k: tune["best"][k] for k in ("seg_per_sm", "warp_mask")}},
+                   "schedule": {k: tune["best"][k] for k in ("seg_per_sm", "warp_mask", "flags")}},
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -119,8 +119,15 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
             ctx->own_stream = true;
         }
     }
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (const char *v = getenv("GLS_CLASS_PRIORITY")) ctx->class_priority = strtoul(v, nullptr, 0) != 0;
+    if (const char *v = getenv("GLS_WIDE_FIRST")) ctx->wide_first = strtoul(v, nullptr, 0) != 0;
     for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
+        // two sets: default priority, and priority rising with fan-in (a schedule option)
+        const int prio = c >= 2 ? prio_hi : (c == 1 ? (prio_lo + prio_hi) / 2 : prio_lo);
         e = cudaStreamCreateWithFlags(&ctx->side[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->side_prio[c], cudaStreamNonBlocking, prio);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev[c], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
@@ -252,6 +259,7 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (int c = 0; c < kClasses; ++c) {
         if (ctx->side[c]) cudaStreamDestroy(ctx->side[c]);
+        if (ctx->side_prio[c]) cudaStreamDestroy(ctx->side_prio[c]);
         if (ctx->join_ev[c]) cudaEventDestroy(ctx->join_ev[c]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
@@ -796,13 +804,16 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
         const bool fork = ctx->concurrent && !(prof && ctx->opts.profile) && n_cls > 1;
         if (fork) CK(cudaEventRecord(ctx->fork_ev, ctx->stream), "fork");
         bool first = true;
-        for (int c = 0; c < kClasses; ++c) {
+        for (int ci = 0; ci < kClasses; ++ci) {
+            // wider gates first when the classes run together: they carry
+            // the most events per gate, so their chain sets the level's length
+            const int c = (fork && ctx->wide_first) ? kClasses - 1 - ci : ci;
             const uint32_t d0 = ctx->cls_start[(kClasses + 1) * L + c], d1 = ctx->cls_start[(kClasses + 1) * L + c + 1];
             if (d1 <= d0) continue;
             // the first class on the main stream, the others beside it
             cudaStream_t st = ctx->stream;
-            if (fork && !first) {
-                st = ctx->side[c];
+            if (fork && (!first || ctx->class_priority)) {
+                st = ctx->class_priority ? ctx->side_prio[c] : ctx->side[c];
                 CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
             }
             launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, st);
@@ -1046,12 +1057,12 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
     const WinDev *dw = ctx->dwave.as<WinDev>();
     if (o.use_graph && nwin > 1) {
         // one graph per wave shape; the descriptors it reads are rewritten per wave
-        const uint64_t key = (uint64_t)nwin | ((uint64_t)max_stim << 11) | ((uint64_t)ctx->warp_mask << 43) |
-                             ((uint64_t)ctx->opts.alloc_mode << 46) | ((uint64_t)ctx->seg_per_sm << 48);
+        gls_ctx::WaveGraph key{nwin, max_stim, ctx->warp_mask, (uint32_t)ctx->opts.alloc_mode, ctx->seg_per_sm,
+                               ctx->class_priority ? 1u : 0u, nullptr, 0};
         cudaGraphExec_t ge = nullptr;
         uint32_t l = 0;
         for (auto &g : ctx->graphs)
-            if (g.key == key) {
+            if (g.same(key)) {
                 ge = g.exec;
                 l = g.launches;
             }
@@ -1068,7 +1079,9 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
             if (g) cudaGraphDestroy(g);
             if (rc) return rc;
             if (e != cudaSuccess) return fail(ctx, GLS_ECUDA, "capture wave graph: %s", cudaGetErrorString(e));
-            ctx->graphs.push_back({key, ge, l});
+            key.exec = ge;
+            key.launches = l;
+            ctx->graphs.push_back(key);
         }
         CK(cudaGraphLaunch(ge, ctx->stream), "graph launch");
         acc.launches += l;
@@ -1152,13 +1165,15 @@ extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
     return GLS_OK;
 }
 
-extern "C" int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask)
+extern "C" int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask, uint32_t flags)
 {
     if (!ctx) return GLS_EINVAL;
-    if (seg_per_sm < 64 || seg_per_sm > 65536 || warp_mask > 7)
-        return fail(ctx, GLS_EINVAL, "schedule out of range: %u segments per SM, warp mask %u", seg_per_sm, warp_mask);
+    if (seg_per_sm < 64 || seg_per_sm > 65536 || warp_mask > 7 || flags > 1)
+        return fail(ctx, GLS_EINVAL, "schedule out of range: %u segments per SM, warp mask %u, flags %u", seg_per_sm,
+                    warp_mask, flags);
     ctx->seg_per_sm = seg_per_sm;
     ctx->warp_mask = warp_mask;
+    ctx->class_priority = flags & GLS_SCHED_CLASS_PRIORITY;
     ctx_drop_graphs(ctx);
     return GLS_OK;
 }
@@ -1177,6 +1192,7 @@ extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_r
     // which fan-in classes run warp-per-segment
     static const uint32_t kSegs[] = {1024, 2048, 4096};
     static const uint32_t kMasks[] = {0, 1, 7};
+    static const uint32_t kFlags[] = {0, GLS_SCHED_CLASS_PRIORITY};
     gls_tune_result r;
     std::memset(&r, 0, sizeof r);
     float best = 1e30f;
@@ -1184,35 +1200,46 @@ extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_r
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
     const uint32_t keep_segs = ctx->seg_per_sm, keep_mask = ctx->warp_mask;
-    for (uint32_t ms_i = 0; ms_i < 3 && rc == GLS_OK; ++ms_i) {
-        for (uint32_t s_i = 0; s_i < 3 && rc == GLS_OK; ++s_i) {
-            ctx->seg_per_sm = kSegs[s_i];
-            ctx->warp_mask = kMasks[ms_i];
-            RunAcc acc;
-            float t = 0.f;
-            // the first run of a shape captures its graph: time the second
-            for (int rep = 0; rep < 2 && rc == GLS_OK; ++rep) rc = run_wave(ctx, 0, nwin, o, acc, &t, e0, e1);
-            const uint32_t c = ms_i * 3 + s_i;
-            r.ms[c] = t;
-            r.seg_per_sm[c] = kSegs[s_i];
-            r.warp_mask[c] = kMasks[ms_i];
-            if (rc == GLS_OK && t < best) {
-                best = t;
-                r.best = c;
+    const bool keep_prio = ctx->class_priority;
+    uint32_t c = 0;
+    for (uint32_t f_i = 0; f_i < 2 && rc == GLS_OK; ++f_i) {
+        for (uint32_t ms_i = 0; ms_i < 3 && rc == GLS_OK; ++ms_i) {
+            for (uint32_t s_i = 0; s_i < 3 && rc == GLS_OK; ++s_i, ++c) {
+                ctx->seg_per_sm = kSegs[s_i];
+                ctx->warp_mask = kMasks[ms_i];
+                ctx->class_priority = kFlags[f_i] & GLS_SCHED_CLASS_PRIORITY;
+                RunAcc acc;
+                float t = 1e30f;
+                // the first run of a shape captures its graph; the best of the next two counts
+                for (int rep = 0; rep < 3 && rc == GLS_OK; ++rep) {
+                    float tr = 0.f;
+                    rc = run_wave(ctx, 0, nwin, o, acc, &tr, e0, e1);
+                    if (rep) t = std::min(t, tr);
+                }
+                r.ms[c] = t;
+                r.seg_per_sm[c] = kSegs[s_i];
+                r.warp_mask[c] = kMasks[ms_i];
+                r.flags[c] = kFlags[f_i];
+                if (rc == GLS_OK && t < best) {
+                    best = t;
+                    r.best = c;
+                }
             }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    r.n = 9;
+    r.n = c;
     r.windows = nwin;
     if (rc) {
         ctx->seg_per_sm = keep_segs;
         ctx->warp_mask = keep_mask;
+        ctx->class_priority = keep_prio;
         return rc;
     }
     ctx->seg_per_sm = r.seg_per_sm[r.best];
     ctx->warp_mask = r.warp_mask[r.best];
+    ctx->class_priority = r.flags[r.best] & GLS_SCHED_CLASS_PRIORITY;
     if (res) *res = r;
     return GLS_OK;
 }

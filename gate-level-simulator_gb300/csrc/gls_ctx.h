@@ -120,8 +120,11 @@ struct gls_ctx {
     // fan-in classes of a level run concurrently: side streams fork after the
     // plan and join before the link (GLS_SIM_CONCURRENT=0 runs them in turn)
     cudaStream_t side[gls::kClasses] = {};
+    cudaStream_t side_prio[gls::kClasses] = {};   // the same with priority rising with fan-in
     cudaEvent_t fork_ev = nullptr, join_ev[gls::kClasses] = {};
     bool concurrent = true;
+    bool wide_first = false;         // launch the widest fan-in class first (GLS_WIDE_FIRST)
+    bool class_priority = false;     // wider classes on higher-priority side streams (GLS_CLASS_PRIORITY)
     bool pipeline = true;            // with concurrent classes: each class links and copies on its own stream
     uint32_t copy_lanes = 8;         // lanes per segment of the copy kernel (GLS_COPY_LANES: 4, 8, 16, 32)
     int sm_count = 0;
@@ -165,9 +168,14 @@ struct gls_ctx {
     DevBuf wave_e;                   // per level: a wave's fan-in events per class
     std::vector<DevBuf> spare_bufs;  // device buffers of windows that ran saif_only, reused by later windows
     struct WaveGraph {
-        uint64_t key;
+        uint32_t nwin, max_stim, warp_mask, alloc_mode, seg_per_sm, class_priority;
         cudaGraphExec_t exec;
         uint32_t launches;
+        bool same(const WaveGraph &o) const
+        {
+            return nwin == o.nwin && max_stim == o.max_stim && warp_mask == o.warp_mask &&
+                   alloc_mode == o.alloc_mode && seg_per_sm == o.seg_per_sm && class_priority == o.class_priority;
+        }
     };
     std::vector<WaveGraph> graphs;
 };

@@ -75,7 +75,8 @@ class BatchOpts(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("n", C.c_uint32), ("best", C.c_uint32), ("windows", C.c_uint32),
-                ("seg_per_sm", C.c_uint32 * 16), ("warp_mask", C.c_uint32 * 16), ("ms", C.c_float * 16)]
+                ("seg_per_sm", C.c_uint32 * 32), ("warp_mask", C.c_uint32 * 32), ("flags", C.c_uint32 * 32),
+                ("ms", C.c_float * 32)]
 
 
 class PresizeModel(C.Structure):
@@ -130,7 +131,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64]
     lib.gls_run_batched.argtypes = [C.c_void_p, C.POINTER(BatchOpts)]
     lib.gls_autotune.argtypes = [C.c_void_p, C.POINTER(BatchOpts), C.POINTER(TuneResult)]
-    lib.gls_set_schedule.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
+    lib.gls_set_schedule.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
     lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
     lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -252,11 +253,12 @@ class Simulator:
         o = BatchOpts(max_wave, 1 if use_graph else 0, 1 if saif_only else 0)
         r = TuneResult()
         self._check(self.lib.gls_autotune(self.h, C.byref(o), C.byref(r)), "autotune")
-        cands = [{"seg_per_sm": r.seg_per_sm[k], "warp_mask": r.warp_mask[k], "ms": r.ms[k]} for k in range(r.n)]
+        cands = [{"seg_per_sm": r.seg_per_sm[k], "warp_mask": r.warp_mask[k], "flags": r.flags[k], "ms": r.ms[k]}
+                 for k in range(r.n)]
         return {"best": cands[r.best], "windows": r.windows, "candidates": cands}
 
-    def set_schedule(self, seg_per_sm: int, warp_mask: int):
-        self._check(self.lib.gls_set_schedule(self.h, seg_per_sm, warp_mask), "set_schedule")
+    def set_schedule(self, seg_per_sm: int, warp_mask: int, flags: int = 0):
+        self._check(self.lib.gls_set_schedule(self.h, seg_per_sm, warp_mask, flags), "set_schedule")
 
     def saif(self, window: int = 0) -> np.ndarray:
         """(n_nets, 3) uint64: T0, T1, TX; UINT64_MAX rows were not produced."""

@@ -185,25 +185,28 @@ typedef struct {
 int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts);
 
 /* Autotuner: runs the first wave of the added windows (as gls_run_batched
- * would form it) under every candidate schedule -- time segments per SM for
- * the thread-per-segment gate kernel (1024, 2048, 4096) times the fan-in
- * classes that run warp-per-segment (none, 1-input, 1- to 3-input) -- and
- * keeps the fastest for the context's later runs.  Results never depend on
- * the schedule. */
+ * would form it; a single window works too) under every candidate schedule
+ * -- time segments per SM for the thread-per-segment gate kernel (1024,
+ * 2048, 4096) times the fan-in classes that run warp-per-segment (none,
+ * 1-input, 1- to 3-input) times plain or priority class streams -- and keeps
+ * the fastest for the context's later runs.  Results never depend on the
+ * schedule. */
+#define GLS_SCHED_CLASS_PRIORITY 1u   /* wider fan-in classes on higher-priority streams */
 typedef struct {
     uint32_t n;               /* candidates tried */
     uint32_t best;            /* index of the one kept */
     uint32_t windows;         /* windows in the timed wave */
-    uint32_t seg_per_sm[16];
-    uint32_t warp_mask[16];
-    float ms[16];             /* device time of the wave under each */
+    uint32_t seg_per_sm[32];
+    uint32_t warp_mask[32];
+    uint32_t flags[32];       /* GLS_SCHED_* */
+    float ms[32];             /* device time of the wave under each (best of two runs) */
 } gls_tune_result;
 int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_result *res);
 /* Set the schedule by hand (e.g. one gls_autotune found for another context
  * on the same netlist): time segments per SM for the thread-per-segment gate
- * kernel (64..65536), and which fan-in classes run warp-per-segment (bits
- * 0-2 for 1-, 2- and 3-input gates). */
-int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask);
+ * kernel (64..65536), which fan-in classes run warp-per-segment (bits 0-2
+ * for 1-, 2- and 3-input gates), and GLS_SCHED_* flags. */
+int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask, uint32_t flags);
 
 /* T0 / T1 / TX per net for a window (arrays of n_nets).  Nets the run did
  * not produce read UINT64_MAX.  Replaces the SAIF integrals of

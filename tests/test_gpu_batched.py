@@ -125,7 +125,7 @@ def test_autotune_keeps_results(design, gpu):
         s.load(nl)
         ids = [s.add_window(st, 0, t_end) for st, t_end in wins]
         t = s.autotune(max_wave=4)
-        assert len(t["candidates"]) == 9 and t["windows"] == 4
+        assert len(t["candidates"]) == 18 and t["windows"] == 4
         assert t["best"]["ms"] == min(c["ms"] for c in t["candidates"])
         s.run_batched(max_wave=4)
         for w, (la, sa) in zip(ids, ref):

@@ -82,7 +82,8 @@ def test_gpu_pool_offsets_past_2_34_events(gpu, oracle_bin):
 
 @pytest.mark.parametrize("knobs", [{"GLS_SIM_CONCURRENT": "0"}, {"GLS_SIM_PIPELINE": "0"},
                                    {"GLS_COPY_LANES": "4"}, {"GLS_COPY_LANES": "16"}, {"GLS_COPY_LANES": "32"},
-                                   {"profile": True}, {"schedule": (512, 7)}, {"schedule": (8192, 1)}])
+                                   {"profile": True}, {"schedule": (512, 7, 0)}, {"schedule": (8192, 1, 1)},
+                                   {"schedule": (2048, 0, 1)}])
 def test_gpu_schedules_and_streams_agree(knobs, gpu, oracle_bin):
     """Results never depend on how a level is scheduled: fan-in classes in
     turn or concurrently, link and copy per class or per level, lanes per
