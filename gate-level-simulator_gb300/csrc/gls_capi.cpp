@@ -244,6 +244,7 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     ctx->meta.release(); ctx->arcs.release(); ctx->ndel.release(); ctx->lut.release(); ctx->slut.release();
     ctx_drop_graphs(ctx);
     ctx->hwave.release();
+    ctx->pin_out.release();
     ctx->dwave.release();
     ctx->wave_e.release();
     free_spares(ctx);
@@ -1257,8 +1258,13 @@ extern "C" int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint
     Window *w = get_done(ctx, window);
     if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
     cudaSetDevice(ctx->opts.device);
-    std::vector<uint64_t> buf((size_t)ctx->n_nets * 3);
-    CK(cudaMemcpy(buf.data(), w->saif.p, buf.size() * 8, cudaMemcpyDeviceToHost), "read saif");
+    // through pinned staging: a pageable destination would go through the
+    // driver's bounce buffers at a fraction of the link's speed
+    const size_t bytes = (size_t)ctx->n_nets * 24;
+    if (!ctx->pin_out.ensure(bytes)) return fail(ctx, GLS_ENOMEM, "pinned staging for SAIF counts");
+    CK(cudaMemcpyAsync(ctx->pin_out.p, w->saif.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "read saif");
+    CK(cudaStreamSynchronize(ctx->stream), "read saif");
+    const uint64_t *buf = ctx->pin_out.as<uint64_t>();
     for (uint32_t n = 0; n < ctx->n_nets; ++n) {
         t0[n] = buf[3ull * n];
         t1[n] = buf[3ull * n + 1];
@@ -1273,7 +1279,11 @@ extern "C" int gls_waveform_lengths(gls_ctx *ctx, uint32_t window, uint32_t *len
     Window *w = get_done(ctx, window);
     if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
     cudaSetDevice(ctx->opts.device);
-    CK(cudaMemcpy(len, w->net_len.p, (size_t)ctx->n_nets * 4, cudaMemcpyDeviceToHost), "read lengths");
+    const size_t bytes = (size_t)ctx->n_nets * 4;
+    if (!ctx->pin_out.ensure(bytes)) return fail(ctx, GLS_ENOMEM, "pinned staging for lengths");
+    CK(cudaMemcpyAsync(ctx->pin_out.p, w->net_len.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "read lengths");
+    CK(cudaStreamSynchronize(ctx->stream), "read lengths");
+    std::memcpy(len, ctx->pin_out.p, bytes);
     return GLS_OK;
 }
 

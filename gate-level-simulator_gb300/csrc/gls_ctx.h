@@ -164,6 +164,7 @@ struct gls_ctx {
     // batched runs: the wave's window descriptors (host pinned, device) and
     // the captured launch graphs, one per wave shape
     PinBuf hwave;
+    PinBuf pin_out;                  // staging of SAIF counts and lengths read back to the host
     DevBuf dwave;
     DevBuf wave_e;                   // per level: a wave's fan-in events per class
     std::vector<DevBuf> spare_bufs;  // device buffers of windows that ran saif_only, reused by later windows
