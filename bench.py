@@ -246,7 +246,12 @@ def gls_arm(args):
         if world > 1:
             torch.distributed.barrier()
 
-    tune = sim.autotune()   # untimed: the schedule for this workload (results never depend on it)
+    if args.schedule:   # a fixed schedule (profiling cases): no autotuning launches
+        seg_sm, mask, flags = (int(x) for x in args.schedule.split(","))
+        sim.set_schedule(seg_sm, mask, flags)
+        tune = {"best": {"seg_per_sm": seg_sm, "warp_mask": mask, "flags": flags}, "candidates": []}
+    else:
+        tune = sim.autotune()   # untimed: the schedule for this workload (results never depend on it)
     log(f"autotune: {tune['best']}; candidates (segments/SM, warp mask, flags: ms): " +
         ", ".join(f"{c['seg_per_sm']}/{c['warp_mask']}/{c['flags']}: {c['ms']:.2f}" for c in tune["candidates"]))
     for _ in range(args.warmup):
@@ -516,6 +521,8 @@ def main():
     ap.add_argument("--depth", type=int, default=None, help="override the logic depth (profiling cases)")
     ap.add_argument("--cycles", type=int, default=None, help="override the cycle count (profiling cases)")
     ap.add_argument("--windows", type=int, default=None, help="c4: number of windows (default 256)")
+    ap.add_argument("--schedule", default=None,
+                    help="c1-c3: fixed schedule 'segments_per_sm,warp_mask,flags' instead of autotuning")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

@@ -98,17 +98,17 @@ struct SegRec {             // one time segment of one gate output
     uint32_t region;        // offset of the segment's stack inside the gate's scratch
     uint32_t cnt;           // entries on the segment's local stack
     uint32_t min_o;         // smallest candidate output time in the segment
-    uint32_t fin;           // entries kept after linking
+    uint32_t last;          // the stack's top entry (when cnt > 0): linking reads no scratch for it
 };
 
 struct CopyRec {            // what k_copy does for one segment
     uint64_t src;           // scratch index of the first kept entry
-    uint64_t dst;           // position of that entry in the gate output's list
-    uint32_t n;             // entries to copy
+    uint64_t dst;           // pool index of that entry (bound mode), else its position in the gate output's list
+    uint32_t n;             // entries to copy (k_link keeps the cut count here between its passes)
     uint32_t drv;           // gate output (level-relative)
     unsigned long long cprev;  // clamped time of the final event before this segment's first
     uint32_t pclass;        // value class of that event (0: 0, 1: 1, 2: X or Z)
-    uint32_t pad;
+    uint32_t out_net;       // the gate output's net
 };
 
 struct WinDev {

@@ -512,7 +512,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
         }
     }
     SegRec r;
-    r.region = region; r.cnt = cnt; r.min_o = min_o; r.fin = 0;
+    r.region = region; r.cnt = cnt; r.min_o = min_o; r.last = top;
     w.segs[seg_id] = r;
 }
 
@@ -1058,7 +1058,7 @@ __device__ void sim_segment_warp(const WinDev &w, const LevelArgs &a, const DrvM
     }
     if (lane == 0) {
         SegRec r;
-        r.region = region; r.cnt = cnt; r.min_o = min_o; r.fin = 0;
+        r.region = region; r.cnt = cnt; r.min_o = min_o; r.last = top;
         w.segs[seg_id] = r;
     }
 }
@@ -1163,8 +1163,11 @@ __global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs
         const uint32_t M = min(ex, carry_min);
         if (valid) {
             uint32_t keep = r.cnt;   // stack times increase: cut from the top
-            while (keep > 0 && ev_time(sx[r.region + keep - 1]) >= M) --keep;
-            w.segs[s].fin = keep;
+            if (keep > 0 && ev_time(r.last) >= M) {
+                --keep;
+                while (keep > 0 && ev_time(sx[r.region + keep - 1]) >= M) --keep;
+            }
+            w.copies[s].n = keep;    // until pass B
         }
         carry_min = min(carry_min, __shfl_sync(FULL, x, 0));
     }
@@ -1179,11 +1182,11 @@ __global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs
         uint32_t keep = 0, region = 0, firstv = 0, lastv = 0, lastt = 0;
         if (valid) {
             const SegRec r = w.segs[s];
-            keep = r.fin;
+            keep = w.copies[s].n;
             region = r.region;
             if (keep) {
                 firstv = ev_val(sx[region]);
-                const uint32_t lw = sx[region + keep - 1];
+                const uint32_t lw = keep == r.cnt ? r.last : sx[region + keep - 1];
                 lastv = ev_val(lw);
                 lastt = ev_time(lw);
             }
@@ -1210,12 +1213,12 @@ __global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs
         if (valid) {
             CopyRec c;
             c.src = scr + region + drop;
-            c.dst = pos;
+            c.dst = a.alloc_mode == kAllocBound ? slot + pos : pos;
             c.n = fin;
             c.drv = i;
             c.cprev = fprior ? csh : cprev;
             c.pclass = (uint32_t)(fprior ? ksh : pclass);
-            c.pad = 0;
+            c.out_net = out_net;
             w.copies[s] = c;
         }
         if (bal) carry_v = __shfl_sync(FULL, lastv, 31 - __clz(bal));
@@ -1272,6 +1275,11 @@ __device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, 
     const int pn = __shfl_sync(FULL, cl, last, W);
     if (any) { cprev = cn; pclass = pn; }
 }
+
+#ifndef GLS_COPY_UNROLL
+#define GLS_COPY_UNROLL 8
+#endif
+constexpr int kCopyUnroll = GLS_COPY_UNROLL;   // entries per lane loaded ahead in k_copy
 
 // k_copy: one W-lane group per segment: copy the kept entries from the
 // level scratch into the pool and add their SAIF contributions to the gate
@@ -1339,23 +1347,35 @@ __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs
         uint32_t nmax = n;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
-        const uint64_t dst = live ? w.slot[c.drv] + c.dst : 0;
-        for (uint32_t i0 = 0; i0 < nmax; i0 += W) {
-            const uint32_t i = i0 + sub;
-            const bool v = i < n;
-            uint32_t word = 0;
-            if (v) {
-                word = w.scratch[c.src + i];
-                w.pool[dst + i] = word;
+        const uint64_t dst = !live ? 0 : (a.alloc_mode == kAllocBound ? c.dst : w.slot[c.drv] + c.dst);
+        // kCopyUnroll loads per lane go out before the stores that follow
+        // them: scratch and pool never overlap, and a segment's copy costs
+        // one memory round trip per W * kCopyUnroll entries, not per W
+        const uint32_t *__restrict__ sp = w.scratch + c.src;
+        uint32_t *__restrict__ dp = w.pool + dst;
+        for (uint32_t i0 = 0; i0 < nmax; i0 += W * kCopyUnroll) {
+            uint32_t wd[kCopyUnroll];
+#pragma unroll
+            for (int u = 0; u < kCopyUnroll; ++u) {
+                const uint32_t i = i0 + u * W + sub;
+                wd[u] = i < n ? __ldcs(sp + i) : 0u;   // read once: stream it past L1
             }
-            integrate_group<W>(w, word, v, i0 < n ? n - i0 : 1u, i0 < n, cprev, pclass, acc);
+#pragma unroll
+            for (int u = 0; u < kCopyUnroll; ++u) {
+                const uint32_t ib = i0 + u * W;
+                if (ib >= nmax) break;   // the same for the whole warp
+                const uint32_t i = ib + sub;
+                const bool v = i < n;
+                if (v) dp[i] = wd[u];
+                integrate_group<W>(w, wd[u], v, ib < n ? n - ib : 1u, ib < n, cprev, pclass, acc);
+            }
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
             for (int o = W / 2; o > 0; o >>= 1) acc[k] += __shfl_down_sync(FULL, acc[k], o, W);
         if (sub == 0 && live) {
-            const uint32_t out_net = a.meta[a.lo + c.drv].out_net;
+            const uint32_t out_net = c.out_net;
 #pragma unroll
             for (int k = 0; k < 3; ++k)
                 if (acc[k]) atomicAdd(&w.saif[3ull * out_net + k], acc[k]);
