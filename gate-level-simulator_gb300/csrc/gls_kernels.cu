@@ -1254,26 +1254,44 @@ __global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs
     }
 }
 
+// Window-relative clamped times in 32 bits.  Event times are at most
+// kMaxTime, so max(t, t_begin) - t_begin never exceeds kMaxTime (or is 0
+// when the window starts past every event): with the bounds capped at 2^31
+// the clamp gives the same values as in 64 bits, and a relative time
+// shifted left by 2 still fits 32 bits next to a 2-bit value class.
+struct RelClamp {
+    uint32_t lo, hi;
+    __device__ __forceinline__ RelClamp(unsigned long long b, unsigned long long e)
+        : lo((uint32_t)min(b, 1ull << 31)), hi((uint32_t)min(e, 1ull << 31)) {}
+    __device__ __forceinline__ uint32_t operator()(uint32_t t) const { return min(max(t, lo), hi) - lo; }
+};
+
+__device__ __forceinline__ void saif_add32(uint32_t acc[3], uint32_t cls, uint32_t d)
+{
+    acc[0] += cls == 0 ? d : 0u;
+    acc[1] += cls == 1 ? d : 0u;
+    acc[2] += cls == 2 ? d : 0u;
+}
+
 // SAIF contributions of W consecutive events of a list held one per lane of
 // a W-lane group: an event holds the net from its time to the next event's,
-// clipped to [t_begin, t_end) (src/simulate.cpp:102-163).  (cprev, pclass)
-// describe the event before the group's first and are advanced past its last.
+// clipped to [t_begin, t_end) (src/simulate.cpp:102-163).  `prev` is the
+// event before the group's first as (relative clamped time << 2 | value
+// class) and is advanced past its last.  The sums of one segment or one
+// list are at most one window long, so they fit 32 bits.
 template <int W>
-__device__ __forceinline__ void integrate_group(const WinDev &w, uint32_t word, bool v, uint32_t n_here, bool any,
-                                                unsigned long long &cprev, int &pclass, unsigned long long acc[3])
+__device__ __forceinline__ void integrate_group(const RelClamp &rc, uint32_t word, bool v, uint32_t n_here, bool any,
+                                                uint32_t &prev, uint32_t acc[3])
 {
     const unsigned FULL = 0xffffffffu;
     const int sub = threadIdx.x & (W - 1);
-    const unsigned long long ct = clampt(ev_time(word), w.t_begin, w.t_end);
-    const int cl = vclass(ev_val(word));
-    unsigned long long cp = __shfl_up_sync(FULL, ct, 1, W);
-    int pc = __shfl_up_sync(FULL, cl, 1, W);
-    if (sub == 0) { cp = cprev; pc = pclass; }
-    if (v) saif_add(acc, pc, ct - cp);
+    const uint32_t me = (rc(ev_time(word)) << 2) | (uint32_t)vclass(ev_val(word));
+    uint32_t pv = __shfl_up_sync(FULL, me, 1, W);
+    if (sub == 0) pv = prev;
+    if (v) saif_add32(acc, pv & 3u, (me >> 2) - (pv >> 2));
     const int last = (int)min((uint32_t)(W - 1), n_here - 1);
-    const unsigned long long cn = __shfl_sync(FULL, ct, last, W);
-    const int pn = __shfl_sync(FULL, cl, last, W);
-    if (any) { cprev = cn; pclass = pn; }
+    const uint32_t nx = __shfl_sync(FULL, me, last, W);
+    if (any) prev = nx;
 }
 
 #ifndef GLS_COPY_UNROLL
@@ -1339,9 +1357,11 @@ __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs
         const CopyRec nx = fetch(s + stride, nw);
         const WinDev &w = ws.get(cw);
         const bool live = s < nseg && c.n > 0;
-        unsigned long long acc[3] = {0, 0, 0};
-        unsigned long long cprev = c.cprev;
-        int pclass = (int)c.pclass;
+        const RelClamp rc(w.t_begin, w.t_end);
+        uint32_t acc[3] = {0, 0, 0};
+        // c.cprev is a clamped absolute time: at most kMaxTime unless the
+        // window starts past every event (then it is t_begin, relative 0)
+        uint32_t prev = (rc((uint32_t)min(c.cprev, (unsigned long long)kMaxTime)) << 2) | c.pclass;
         const uint32_t n = live ? c.n : 0;
         // groups of one warp may have different lengths: loop to the warp's longest
         uint32_t nmax = n;
@@ -1367,7 +1387,7 @@ __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs
                 const uint32_t i = ib + sub;
                 const bool v = i < n;
                 if (v) dp[i] = wd[u];
-                integrate_group<W>(w, wd[u], v, ib < n ? n - ib : 1u, ib < n, cprev, pclass, acc);
+                integrate_group<W>(rc, wd[u], v, ib < n ? n - ib : 1u, ib < n, prev, acc);
             }
         }
 #pragma unroll
@@ -1378,7 +1398,7 @@ __global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs
             const uint32_t out_net = c.out_net;
 #pragma unroll
             for (int k = 0; k < 3; ++k)
-                if (acc[k]) atomicAdd(&w.saif[3ull * out_net + k], acc[k]);
+                if (acc[k]) atomicAdd(&w.saif[3ull * out_net + k], (unsigned long long)acc[k]);
         }
         c = nx;
         cw = nw;
@@ -1397,23 +1417,25 @@ __global__ void __launch_bounds__(256) k_stim_saif(const WinSet<kBatch> ws)
     const uint32_t net = w.stim_nets[i];
     const uint64_t off = w.net_off[net];
     const uint32_t len = w.net_len[net];
-    unsigned long long cprev = w.t_begin;
-    int pclass = 2;
-    unsigned long long acc[3] = {0, 0, 0};
+    const RelClamp rc(w.t_begin, w.t_end);
+    uint32_t prev = 2u;   // before the first event: X from t_begin
+    uint32_t acc[3] = {0, 0, 0};
     for (uint32_t i0 = 0; i0 < len; i0 += 32) {
         const bool v = i0 + lane < len;
         const uint32_t word = v ? w.pool[off + i0 + lane] : 0u;
-        integrate_group<32>(w, word, v, len - i0, true, cprev, pclass, acc);
+        integrate_group<32>(rc, word, v, len - i0, true, prev, acc);
     }
-    if (lane == 0) saif_add(acc, pclass, w.t_end - cprev);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
     if (lane == 0) {
-        w.saif[3ull * net + 0] = acc[0];
-        w.saif[3ull * net + 1] = acc[1];
-        w.saif[3ull * net + 2] = acc[2];
+        // the last event holds until t_end
+        unsigned long long tot[3] = {acc[0], acc[1], acc[2]};
+        saif_add(tot, (int)(prev & 3u), w.t_end - (w.t_begin + (prev >> 2)));
+        w.saif[3ull * net + 0] = tot[0];
+        w.saif[3ull * net + 1] = tot[1];
+        w.saif[3ull * net + 2] = tot[2];
     }
 }
 
