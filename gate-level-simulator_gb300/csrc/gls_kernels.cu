@@ -195,11 +195,51 @@ template <> struct WinSet<true> {
     __device__ __forceinline__ uint32_t size() const { return n; }
 };
 
+// Exclusive block-wide scan of three quantities at once (two barriers for
+// the three); *t* receive the block totals.
+__device__ void block_excl_scan3(uint32_t &x, unsigned long long &y, unsigned long long &z, uint32_t &tx,
+                                 unsigned long long &ty, unsigned long long &tz, uint32_t *sx,
+                                 unsigned long long *sy, unsigned long long *sz)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t ix = x;
+    unsigned long long iy = y, iz = z;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ux = __shfl_up_sync(FULL, ix, o);
+        const unsigned long long uy = __shfl_up_sync(FULL, iy, o), uz = __shfl_up_sync(FULL, iz, o);
+        if (lane >= o) { ix += ux; iy += uy; iz += uz; }
+    }
+    if (lane == 31) { sx[wid] = ix; sy[wid] = iy; sz[wid] = iz; }
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t vx = lane < nw ? sx[lane] : 0u;
+        unsigned long long vy = lane < nw ? sy[lane] : 0ull, vz = lane < nw ? sz[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ux = __shfl_up_sync(FULL, vx, o);
+            const unsigned long long uy = __shfl_up_sync(FULL, vy, o), uz = __shfl_up_sync(FULL, vz, o);
+            if (lane >= o) { vx += ux; vy += uy; vz += uz; }
+        }
+        sx[lane] = vx; sy[lane] = vy; sz[lane] = vz;
+    }
+    __syncthreads();
+    const uint32_t px = wid ? sx[wid - 1] : 0u;
+    const unsigned long long py = wid ? sy[wid - 1] : 0ull, pz = wid ? sz[wid - 1] : 0ull;
+    tx = sx[31]; ty = sy[31]; tz = sz[31];
+    __syncthreads();   // the arrays are reused by the next call
+    x = px + ix - x; y = py + iy - y; z = pz + iz - z;
+}
+
+// gate outputs per thread in one round of k_plan's first pass (their loads overlap)
+constexpr int kPlanPer = 4;
+
 // one block per window
 template <bool kBatch>
 __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArgs a)
 {
-    __shared__ unsigned long long sm64[32];
+    __shared__ unsigned long long sm64[32], sm64b[32], s_sum[kClasses + 1];
     __shared__ uint32_t sm32[32];
     __shared__ uint32_t s_seg[kClasses];
     __shared__ unsigned long long s_base;
@@ -210,30 +250,50 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         if (threadIdx.x == 0) *w.n_segs = 0;
         return;
     }
-    // fan-in events of the level per fan-in class: every class runs as its
-    // own launch, so every class is split into about seg_target segments
+    if (threadIdx.x <= kClasses) s_sum[threadIdx.x] = 0;
+    // Pass 1: every gate output's fan-in events E and fan-in class, parked
+    // in its slot entry as E << 2 | class (and its output net in its scratch
+    // entry) until pass 2 overwrites both; the level's fan-in events per
+    // class (every class runs as its own launch, so every class is split
+    // into about seg_target segments) and its gate events.
+    const uint32_t step = blockDim.x * kPlanPer;
     unsigned long long e_cls[kClasses] = {0, 0, 0, 0}, g_tot = 0;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const DrvMeta &md = a.meta[a.lo + i];
-        unsigned long long E = 0;
-        for (int j = 0; j < md.m; ++j) E += w.net_len[md.net[j]];
-        const int c = fanin_class(md.m);
+    for (uint32_t r = 0; r < n; r += step) {
 #pragma unroll
-        for (int k = 0; k < kClasses; ++k) if (k == c) e_cls[k] += E;
-        if (md.flags & kFlagFirstOut) {  // first output of its instance: count fan-in per pin
-            for (int p = 0; p < md.n_pins; ++p) g_tot += w.net_len[md.net[(md.pin_slot >> (3 * p)) & 7u]];
+        for (int k = 0; k < kPlanPer; ++k) {
+            const uint32_t i = r + k * blockDim.x + threadIdx.x;
+            if (i >= n) break;
+            const DrvMeta &md = a.meta[a.lo + i];
+            const int m = md.m;
+            unsigned long long E = 0;
+#pragma unroll
+            for (int j = 0; j < kMaxSlots; ++j)
+                if (j < m) E += w.net_len[md.net[j]];
+            const int c = fanin_class(m);
+#pragma unroll
+            for (int q = 0; q < kClasses; ++q) if (q == c) e_cls[q] += E;
+            if (md.flags & kFlagFirstOut) {  // first output of its instance: count fan-in per pin
+                for (int p = 0; p < md.n_pins; ++p) g_tot += w.net_len[md.net[(md.pin_slot >> (3 * p)) & 7u]];
+            }
+            w.slot[i] = (E << 2) | (unsigned long long)c;
+            w.scr[i] = md.out_net;
         }
     }
-    unsigned long long tot, e_tot = 0;
+    __syncthreads();   // s_sum cleared
+    {
+        const unsigned FULL = 0xffffffffu;
 #pragma unroll
-    for (int k = 0; k < kClasses; ++k) {
-        block_excl_scan<unsigned long long>(e_cls[k], &tot, sm64);
-        e_cls[k] = tot;
-        e_tot += tot;
+        for (int q = 0; q <= kClasses; ++q) {
+            unsigned long long v = q < kClasses ? e_cls[q] : g_tot;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+            if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_sum[q], v);
+        }
     }
-    block_excl_scan<unsigned long long>(g_tot, &tot, sm64);
-    g_tot = tot;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        unsigned long long e_tot = 0;
+        for (int q = 0; q < kClasses; ++q) e_tot += s_sum[q];
         unsigned long long floor_seg = 8;
         if (w.seg_cap <= n) {
             atomicOr(w.err, kErrSegCap);
@@ -245,12 +305,12 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             unsigned long long seg = a.seg_events;
             const bool warp = (a.warp_mask >> k) & 1u;
             const unsigned long long target = warp ? a.seg_target_w : a.seg_target;
-            const unsigned long long ev = a.wave_e ? a.wave_e[k] : e_cls[k];   // the wave shares the GPU
+            const unsigned long long ev = a.wave_e ? a.wave_e[k] : s_sum[k];   // the wave shares the GPU
             if (!seg) seg = max(warp ? 128ull : 32ull, (ev + target - 1) / max(1ull, target));
             s_seg[k] = (uint32_t)min(max(seg, floor_seg), 0x7FFFFFFFull);
         }
         s_base = *w.top;
-        atomicAdd(&w.counters[0], g_tot);
+        atomicAdd(&w.counters[0], s_sum[kClasses]);
         atomicAdd(&w.counters[3], e_tot);
     }
     __syncthreads();
@@ -259,18 +319,20 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         if (threadIdx.x == 0) *w.n_segs = 0;
         return;
     }
+    // Pass 2: segments, slot and scratch sizes, placed by a block scan in
+    // gate-output order
     const unsigned long long base = s_base;
     uint32_t run_seg = 0;
     unsigned long long run_slot = 0, run_scr = 0;
-    for (uint32_t c = 0; c < n; c += blockDim.x) {
-        const uint32_t i = c + threadIdx.x;
-        uint32_t S = 0;
+    for (uint32_t r = 0; r < n; r += blockDim.x) {
+        const uint32_t i = r + threadIdx.x;
+        uint32_t S = 0, onet = 0;
         unsigned long long slot = 0, scr = 0;
         if (i < n) {
-            const DrvMeta &md = a.meta[a.lo + i];
-            unsigned long long E = 0;
-            for (int j = 0; j < md.m; ++j) E += w.net_len[md.net[j]];
-            const uint32_t seg = s_seg[fanin_class(md.m)];
+            const unsigned long long ec = w.slot[i];
+            onet = (uint32_t)w.scr[i];
+            const unsigned long long E = ec >> 2;
+            const uint32_t seg = s_seg[ec & 3u];
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
             slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
             if (a.alloc_mode == kAllocExact) slot = 0;
@@ -278,17 +340,15 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             if (a.alloc_mode != kAllocBound) w.res[i] = (uint32_t)slot;
             scr = (E + S + 3) & ~3ull;      // segment stacks: events of the segment (+1 for the first)
         }
-        uint32_t tS;
-        unsigned long long tSlot, tScr;
-        const uint32_t xs = block_excl_scan<uint32_t>(S, &tS, sm32);
-        const unsigned long long xo = block_excl_scan<unsigned long long>(slot, &tSlot, sm64);
-        const unsigned long long xc = block_excl_scan<unsigned long long>(scr, &tScr, sm64);
+        uint32_t xs = S, tS;
+        unsigned long long xo = slot, xc = scr, tSlot, tScr;
+        block_excl_scan3(xs, xo, xc, tS, tSlot, tScr, sm32, sm64, sm64b);
         if (i < n) {
             w.seg_base[i] = run_seg + xs;
             const unsigned long long st = base + run_slot + xo;
             w.slot[i] = st;
             w.scr[i] = run_scr + xc;
-            w.net_off[a.meta[a.lo + i].out_net] = st;
+            w.net_off[onet] = st;
         }
         run_seg += tS;
         run_slot += tSlot;
