@@ -470,6 +470,79 @@ __device__ __forceinline__ uint32_t slut_get(const uint4 &t, uint32_t curp)
     return (wd >> (2 * (x & 15u))) & 3u;
 }
 
+// Time of the merged event of rank r (0-based) of two event lists X and Y
+// (r < nx + ny), found by a merge-path search galloping from the guess g for
+// the number of X events among the first r; on return ix / iy are the
+// first events of X / Y at or after that time.  Equal times may sit in both
+// lists (not within one), so a cut at the returned time keeps every time's
+// events on one side.
+__device__ __forceinline__ uint32_t rank_time2(const uint32_t *__restrict__ X, uint32_t nx,
+                                               const uint32_t *__restrict__ Y, uint32_t ny, uint32_t r, uint32_t g,
+                                               uint32_t &ix, uint32_t &iy)
+{
+    // short(i): the first r merged events hold more than i events of X
+    // (true for small i, false from the answer on)
+    auto short_x = [&](uint32_t i) { return i < nx && r - i > 0 && ev_time(Y[r - i - 1]) > ev_time(X[i]); };
+    const uint32_t lo0 = r > ny ? r - ny : 0u, hi0 = min(r, nx);
+    g = min(max(g, lo0), hi0);
+    uint32_t lo, hi;   // the answer lies in [lo, hi]
+    if (short_x(g)) {
+        uint32_t a = g, step = 1;
+        for (;;) {
+            const uint32_t b = a + step;
+            if (b >= hi0) { lo = a + 1; hi = hi0; break; }
+            if (!short_x(b)) { lo = a + 1; hi = b; break; }
+            a = b;
+            step <<= 1;
+        }
+    } else {
+        uint32_t b = g, step = 1;
+        for (;;) {
+            if (b - lo0 < step) { lo = lo0; hi = b; break; }
+            const uint32_t a = b - step;
+            if (short_x(a)) { lo = a + 1; hi = b; break; }
+            b = a;
+            step <<= 1;
+        }
+    }
+    while (lo < hi) {
+        const uint32_t mid = lo + ((hi - lo) >> 1);
+        if (short_x(mid)) lo = mid + 1; else hi = mid;
+    }
+    const uint32_t i = lo, j = r - lo;
+    const uint32_t tx = i < nx ? ev_time(X[i]) : kInf, ty = j < ny ? ev_time(Y[j]) : kInf;
+    const uint32_t T = min(tx, ty);
+    ix = i - ((i > 0 && ev_time(X[i - 1]) == T) ? 1u : 0u);
+    iy = j - ((j > 0 && ev_time(Y[j - 1]) == T) ? 1u : 0u);
+    return T;
+}
+
+// Cut sk of S (0 < sk < S) of a gate output's fan-in timeline: the time of
+// the event of rank sk * (plen + slen) / S in the merge of its two longest
+// input lists (piv, sec), so that those two (all of them for gates with two
+// input nets) split into segments of equal size; with one input net the
+// event of rank sk * plen / S of that list.  cut[j] receives list j's first
+// event at or after that time.  The cut time does not decrease with sk.
+template <int M>
+__device__ __forceinline__ void cut_at(const uint32_t *__restrict__ pool, const uint64_t (&off)[M],
+                                       const uint32_t (&len)[M], int m, int piv, int sec, uint64_t poff, uint64_t soff,
+                                       uint32_t plen, uint32_t slen, uint32_t sk, uint32_t S, uint32_t (&cut)[M])
+{
+    uint32_t ip, is = 0, T;
+    if (sec >= 0) {
+        const uint32_t r = mul_div(sk, plen + slen, S);
+        T = rank_time2(pool + poff, plen, pool + soff, slen, r, mul_div(r, plen, plen + slen), ip, is);
+    } else {
+        ip = mul_div(sk, plen, S);
+        T = ev_time(pool[poff + ip]);
+    }
+#pragma unroll
+    for (int j = 0; j < M; ++j) {
+        if (j < m)
+            cut[j] = j == piv ? ip : (j == sec ? is : search_from(pool + off[j], len[j], T, mul_div(ip, len[j], plen)));
+    }
+}
+
 template <int M>
 __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t s,
                             uint32_t S, uint32_t seg_id, uint64_t scr, const uint4 sl)
@@ -478,8 +551,8 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     const uint4 *P = reinterpret_cast<const uint4 *>(w.pool);
     uint64_t off[M];
     uint32_t len[M];
-    int piv = 0;
-    uint32_t plen = 0;
+    int piv = 0, sec = -1;   // the longest input list and the longest of the others
+    uint32_t plen = 0, slen = 0;
 #pragma unroll
     for (int j = 0; j < M; ++j) {
         len[j] = 0; off[j] = 0;
@@ -487,16 +560,21 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
             const uint32_t net = md.net[j];
             off[j] = w.net_off[net];
             len[j] = w.net_len[net];
-            if (len[j] > plen) { plen = len[j]; piv = j; }
+            if (len[j] > plen) { sec = piv; slen = plen; plen = len[j]; piv = j; }
+            else if (sec < 0 || len[j] > slen) { sec = j; slen = len[j]; }
         }
     }
-    uint64_t poff = 0;
+    if (md.m < 2) sec = -1;
+    uint64_t poff = 0, soff = 0;
 #pragma unroll
-    for (int j = 0; j < M; ++j) if (j == piv) poff = off[j];
-    const uint32_t *pt = w.pool + poff;
-    const uint32_t plo = mul_div(s, plen, S), phi = mul_div(s + 1, plen, S);
-    const uint32_t tlo = s > 0 ? ev_time(pt[plo]) : 0u;
-    const uint32_t thi = s + 1 < S ? ev_time(pt[phi]) : kInf;
+    for (int j = 0; j < M; ++j) {
+        if (j == piv) poff = off[j];
+        if (j == sec) soff = off[j];
+    }
+    // the segment's first events (cut s) and end events (cut s + 1)
+    uint32_t cb[M], ce[M];
+    if (s > 0) cut_at<M>(w.pool, off, len, md.m, piv, sec, poff, soff, plen, slen, s, S, cb);
+    if (s + 1 < S) cut_at<M>(w.pool, off, len, md.m, piv, sec, poff, soff, plen, slen, s + 1, S, ce);
     uint32_t curp = 0x555u;   // every slot X
     uint32_t region = s, capn = 1;
     bool before = false;
@@ -506,10 +584,8 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     for (int j = 0; j < M; ++j) {
         uint32_t b = 0, e = 0;
         if (j < md.m) {
-            const uint32_t gl = plen ? mul_div(plo, len[j], plen) : 0u;
-            const uint32_t gh = plen ? mul_div(phi, len[j], plen) : 0u;
-            b = s > 0 ? (j == piv ? plo : search_from(w.pool + off[j], len[j], tlo, gl)) : 0u;
-            e = s + 1 < S ? (j == piv ? phi : search_from(w.pool + off[j], len[j], thi, gh)) : len[j];
+            b = s > 0 ? cb[j] : 0u;
+            e = s + 1 < S ? ce[j] : len[j];
             region += b;
             capn += e - b;
             if (b > 0) {
