@@ -360,9 +360,11 @@ def gls_arm(args):
     sim_ms_step = sim_ms / args.steps
     achieved = sim_bytes / (sim_ms_step / 1000.0) / 1e9
     peak, src = peak_hbm()
+    # DRAM bytes of the k_sim launches of one step, from an ncu capture of
+    # this workload (one-pass metrics; profiles/k_sim_c2-depth6-profiling-case.md)
     traffic = None
     tp = REPO / "profiles" / "k_sim_traffic.json"
-    if tp.exists():
+    if tp.exists() and not (args.cells or args.depth or args.cycles):
         tr = json.loads(tp.read_text())
         if tr.get("workload") == args.config:
             traffic = tr.get("bytes_per_step")
@@ -379,7 +381,10 @@ def gls_arm(args):
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": src,
+                     "frac": achieved / peak, "traffic": traffic,
+                     "traffic_basis": "DRAM bytes per step over the k_sim launches, ncu capture of this workload"
+                                      if traffic else None,
+                     "peak_source": src,
                      "algorithmic_bytes_per_step": sim_bytes,
                      "kernel_ms_per_step": {"k_sim": sim_ms_step, "k_combine": comb_ms / args.steps,
                                             "k_plan": plan_ms / args.steps,
