@@ -248,6 +248,8 @@ extern "C" int gls_destroy(gls_ctx *ctx)
     ctx->dwave.release();
     ctx->wave_e.release();
     free_spares(ctx);
+    delete ctx->pool;
+    ctx->pool = nullptr;
     for (LevelScratch *l : ctx->lsc) {
         l->release();
         delete l;
@@ -619,30 +621,40 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     uint32_t *hw = w->h_words.as<uint32_t>();
     std::atomic<int> bad(0);
     std::atomic<uint32_t> bad_net(0);
+    // The loops carry no early exit so that the compiler vectorizes them; a
+    // net's faults are reported in the order value, time range, time order.
     auto pack = [&](uint32_t k0, uint32_t k1) {
         for (uint32_t k = k0; k < k1; ++k) {
-            const uint64_t a = st->ev_start[k], b = st->ev_start[k + 1];
+            const uint64_t a = st->ev_start[k], cnt = st->ev_start[k + 1] - a;
+            const uint32_t *tt = st->time + a;
+            const uint8_t *vv = st->value + a;
             uint32_t *o = hw + at[k];
-            uint32_t prev = 0;
-            for (uint64_t e = a; e < b; ++e) {
-                const uint32_t t = st->time[e], v = st->value[e];
-                if (v > 3 || t > kMaxTime || (e > a && t <= prev)) {
-                    bad = v > 3 ? 1 : (t > kMaxTime ? 2 : 3);
-                    bad_net = st->net[k];
-                    return;
-                }
-                prev = t;
-                *o++ = ev_word(t, v);
+            uint32_t ev = 0, et = 0, eo = 0;
+            for (uint64_t e = 0; e < cnt; ++e) {
+                const uint32_t t = tt[e], v = vv[e];
+                ev |= v > 3 ? 1u : 0u;
+                et |= t > kMaxTime ? 1u : 0u;
+                o[e] = (t << 2) | (v & 3u);
             }
-            for (uint64_t e = b - a; e < round4(b - a); ++e) *o++ = kInf;
+            for (uint64_t e = 1; e < cnt; ++e) eo |= tt[e] <= tt[e - 1] ? 1u : 0u;
+            for (uint64_t e = cnt; e < round4(cnt); ++e) o[e] = kInf;
+            if (ev | et | eo) {
+                bad = ev ? 1 : (et ? 2 : 3);
+                bad_net = st->net[k];
+                return;
+            }
         }
     };
     const unsigned hc = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    if (total > (1u << 20) && hc > 1 && st->n_nets > hc) {
-        std::vector<std::thread> th;
-        for (unsigned q = 0; q < hc; ++q)
-            th.emplace_back(pack, (uint32_t)((uint64_t)st->n_nets * q / hc), (uint32_t)((uint64_t)st->n_nets * (q + 1) / hc));
-        for (auto &t : th) t.join();
+    if (total > (1u << 20) && hc > 1 && st->n_nets > 4 * hc) {
+        if (!ctx->pool) ctx->pool = new WorkPool(hc - 1);
+        // parts of about equal event counts: part q starts at the first net
+        // whose packed offset reaches q * total / parts
+        const unsigned parts = 4 * ctx->pool->threads();
+        std::vector<uint32_t> first(parts + 1, st->n_nets);
+        for (unsigned q = 0; q < parts; ++q)
+            first[q] = (uint32_t)(std::lower_bound(at.begin(), at.end() - 1, total * q / parts) - at.begin());
+        ctx->pool->parallel_for(parts, [&](unsigned q) { pack(first[q], std::max(first[q], first[q + 1])); });
     } else {
         pack(0, st->n_nets);
     }
@@ -667,7 +679,8 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         const double f = ctx->opts.alloc_mode == GLS_ALLOC_BOUND ? 2.5 : 1.3;
         cap = total + (uint64_t)(f * avg * (double)ctx->pins_total) + 8ull * ctx->n_drv + 1024;
         size_t fr = 0, tot = 0;
-        if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
+        // a reused window that already holds this much needs no limit
+        if (cap + ctx->pool_gap > w->cap && cudaMemGetInfo(&fr, &tot) == cudaSuccess) {
             const uint64_t limit = (uint64_t)(fr * 0.6) / 5;
             if (cap > limit) cap = std::max<uint64_t>(limit, total + 1024);
         }
@@ -1270,6 +1283,21 @@ extern "C" int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint
         t1[n] = buf[3ull * n + 1];
         tx[n] = buf[3ull * n + 2];
     }
+    return GLS_OK;
+}
+
+extern "C" int gls_saif_table(gls_ctx *ctx, uint32_t window, uint64_t *t3)
+{
+    if (!ctx || !t3) return GLS_EINVAL;
+    Window *w = get_done(ctx, window);
+    if (!w) return fail(ctx, GLS_ESTATE, "window %u not simulated", window);
+    cudaSetDevice(ctx->opts.device);
+    // the device keeps the counters in this layout: one copy through pinned staging
+    const size_t bytes = (size_t)ctx->n_nets * 24;
+    if (!ctx->pin_out.ensure(bytes)) return fail(ctx, GLS_ENOMEM, "pinned staging for SAIF counts");
+    CK(cudaMemcpyAsync(ctx->pin_out.p, w->saif.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "read saif");
+    CK(cudaStreamSynchronize(ctx->stream), "read saif");
+    std::memcpy(t3, ctx->pin_out.p, bytes);
     return GLS_OK;
 }
 

@@ -1,13 +1,92 @@
 // Host-side context of libgls, shared by the C ABI translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <condition_variable>
 #include <cstdint>
+#include <functional>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 #include "gls.h"
 #include "gls_internal.h"
 
 namespace glsh {
+
+// Host threads kept for the context's lifetime: parallel_for(n, f) calls
+// f(0) .. f(n-1) on them and on the caller, and returns when all are done.
+// (A call per window would otherwise start and join its threads each time.)
+class WorkPool {
+public:
+    explicit WorkPool(unsigned threads)
+    {
+        for (unsigned i = 0; i < threads; ++i) th_.emplace_back([this] { loop(); });
+    }
+    ~WorkPool()
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    unsigned threads() const { return (unsigned)th_.size() + 1; }
+    void parallel_for(unsigned n, const std::function<void(unsigned)> &f)
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            f_ = &f;
+            n_ = n;
+            next_ = 0;
+            left_ = n;
+            ++gen_;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> l(mu_);
+        done_.wait(l, [this] { return left_ == 0; });
+        f_ = nullptr;
+    }
+
+private:
+    void work()
+    {
+        for (;;) {
+            unsigned i;
+            const std::function<void(unsigned)> *f;
+            {
+                std::lock_guard<std::mutex> l(mu_);
+                if (!f_ || next_ >= n_) return;
+                i = next_++;
+                f = f_;
+            }
+            (*f)(i);
+            std::lock_guard<std::mutex> l(mu_);
+            if (--left_ == 0) done_.notify_all();
+        }
+    }
+    void loop()
+    {
+        uint64_t seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> l(mu_);
+                cv_.wait(l, [&] { return stop_ || (gen_ != seen && f_ && next_ < n_); });
+                if (stop_) return;
+                seen = gen_;
+            }
+            work();
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(unsigned)> *f_ = nullptr;
+    unsigned n_ = 0, next_ = 0, left_ = 0;
+    uint64_t gen_ = 0;
+    bool stop_ = false;
+};
 
 struct DevBuf {
     void *p = nullptr;
@@ -165,6 +244,7 @@ struct gls_ctx {
     // the captured launch graphs, one per wave shape
     PinBuf hwave;
     PinBuf pin_out;                  // staging of SAIF counts and lengths read back to the host
+    WorkPool *pool = nullptr;        // host threads that pack stimuli (made on first use)
     DevBuf dwave;
     DevBuf wave_e;                   // per level: a wave's fan-in events per class
     std::vector<DevBuf> spare_bufs;  // device buffers of windows that ran saif_only, reused by later windows

@@ -700,10 +700,13 @@ __device__ __forceinline__ uint32_t window_of(const uint32_t *s_pre, uint32_t nw
 // next one from a shared counter as they finish, so long and short segments
 // balance inside the block.
 template <int M, bool kBatch>
+#ifndef GLS_SIM2_BLOCKS
+#define GLS_SIM2_BLOCKS 8   // resident blocks per SM the 1- and 2-input gate kernels are compiled for
+#endif
 #ifndef GLS_SIM3_BLOCKS
 #define GLS_SIM3_BLOCKS 6   // resident blocks per SM the 3-input gate kernel is compiled for
 #endif
-__global__ void __launch_bounds__(128, M <= 2 ? 8 : (M == 3 ? GLS_SIM3_BLOCKS : 4))
+__global__ void __launch_bounds__(128, M <= 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4))
     k_sim(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     __shared__ uint32_t s_next;
@@ -1618,7 +1621,7 @@ static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, 
         default: break;
         }
     }
-    const int grid = sm_count * (cls <= 1 ? 8 : (cls == 2 ? GLS_SIM3_BLOCKS : 4));
+    const int grid = sm_count * (cls <= 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4));
     switch (cls) {
     case 0: k_sim<1, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
     case 1: k_sim<2, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;

@@ -24,7 +24,7 @@ MLP_PARAMS = MLP_HID * MLP_IN + MLP_HID + MLP_HID * MLP_HID + MLP_HID + MLP_HID 
 
 # every symbol include/gls.h declares
 EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "gls_add_window",
-            "gls_clear_windows", "gls_run", "gls_saif_counts", "gls_waveform_lengths", "gls_waveform",
+            "gls_clear_windows", "gls_run", "gls_saif_counts", "gls_saif_table", "gls_waveform_lengths", "gls_waveform",
             "gls_stats_get", "gls_cell_lut", "gls_abi_version", "gls_run_level_static",
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
@@ -121,6 +121,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_clear_windows.argtypes = [C.c_void_p]
     lib.gls_run.argtypes = [C.c_void_p]
     lib.gls_saif_counts.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gls_saif_table.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
     lib.gls_waveform_lengths.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
     lib.gls_waveform.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                  C.POINTER(C.c_uint64)]
@@ -262,11 +263,17 @@ class Simulator:
 
     def saif(self, window: int = 0) -> np.ndarray:
         """(n_nets, 3) uint64: T0, T1, TX; UINT64_MAX rows were not produced."""
-        t0 = np.zeros(self.n_nets, np.uint64)
-        t1 = np.zeros(self.n_nets, np.uint64)
-        tx = np.zeros(self.n_nets, np.uint64)
+        t3 = np.empty((self.n_nets, 3), np.uint64)
+        self._check(self.lib.gls_saif_table(self.h, window, _ptr(t3)), "saif_table")
+        return t3
+
+    def saif_counts(self, window: int = 0):
+        """T0, T1, TX as three arrays (the reference-shaped call)."""
+        t0 = np.empty(self.n_nets, np.uint64)
+        t1 = np.empty(self.n_nets, np.uint64)
+        tx = np.empty(self.n_nets, np.uint64)
         self._check(self.lib.gls_saif_counts(self.h, window, _ptr(t0), _ptr(t1), _ptr(tx)), "saif_counts")
-        return np.stack([t0, t1, tx], axis=1)
+        return t0, t1, tx
 
     def lengths(self, window: int = 0) -> np.ndarray:
         ln = np.zeros(self.n_nets, np.uint32)

@@ -213,6 +213,9 @@ int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask, uint
  * src/simulate.cu:174-253, 1592-1677 (serial: src/simulate.cpp:102-163). */
 int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint64_t *t1,
                     uint64_t *tx);
+/* The same counts as one table of n_nets rows (T0, T1, TX): the device's
+ * own layout, read back in one copy.  No counterpart in the reference. */
+int gls_saif_table(gls_ctx *ctx, uint32_t window, uint64_t *t3);
 
 /* Number of events of every net (n_nets), UINT32_MAX where not produced. */
 int gls_waveform_lengths(gls_ctx *ctx, uint32_t window, uint32_t *len);

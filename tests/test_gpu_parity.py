@@ -173,6 +173,38 @@ def test_gpu_rejects_bad_input(gpu):
             s.saif(0)
 
 
+def test_gpu_saif_table_matches_counts(gpu, oracle_bin):
+    """The interleaved SAIF table and the three-array call read the same counts."""
+    nl, st = random_case(7, max_gates=24, max_in=4, horizon=900, max_events=120)
+    ow, osaif, _ = run_oracle(nl, st, 0, 1000)
+    with Simulator() as s:
+        s.load(nl)
+        w = s.add_window(st, 0, 1000)
+        s.run()
+        t3 = s.saif(w)
+        t0, t1, tx = s.saif_counts(w)
+    assert t3.shape == (nl.n_nets, 3)
+    assert np.array_equal(t3, np.stack([t0, t1, tx], axis=1))
+    done = t3[:, 0] != np.iinfo(np.uint64).max
+    assert np.array_equal(t3[done], osaif[done])
+
+
+def test_gpu_rejects_bad_stimulus_values(gpu):
+    """A value above 3 or a time past 2^30-2 is refused when the window is added."""
+    nl = assemble([("GEN_INV_D1", [0], [1], [(2, "i", "zn", 5, 5)])])
+    with Simulator() as s:
+        s.load(nl)
+        bad_v = stimulus({0: [(0, 0), (5, 3)]})
+        bad_v.value[1] = 7
+        with pytest.raises(GlsError, match="value above 3"):
+            s.add_window(bad_v, 0, 10)
+        bad_t = stimulus({0: [(0, 0), (5, 3)]})
+        bad_t.time[1] = (1 << 30) - 1
+        with pytest.raises(GlsError, match="largest event time"):
+            s.add_window(bad_t, 0, 10)
+        s.add_window(stimulus({0: [(0, 0), (5, 3)]}), 0, 10)   # the context stays usable
+
+
 def test_gpu_pool_regrowth(gpu, oracle_bin):
     """A deliberately tiny initial event pool must grow and give the same result."""
     nl, st = random_case(44, max_gates=40, max_in=4, horizon=4000, max_events=400)
