@@ -129,6 +129,8 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         e = cudaStreamCreateWithFlags(&ctx->side[c], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->side_prio[c], cudaStreamNonBlocking, prio);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->link_ev[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->copy_ev[c], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
@@ -144,6 +146,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
     if (const char *v = getenv("GLS_SIM_WARP_MASK")) ctx->warp_mask = (uint32_t)strtoul(v, nullptr, 0) & 7u;
     if (const char *v = getenv("GLS_SIM_CONCURRENT")) ctx->concurrent = strtoul(v, nullptr, 0) != 0;
     if (const char *v = getenv("GLS_SIM_PIPELINE")) ctx->pipeline = strtoul(v, nullptr, 0) != 0;
+    if (const char *v = getenv("GLS_PLAN_OVERLAP")) ctx->plan_overlap = strtoul(v, nullptr, 0) != 0;
     if (const char *v = getenv("GLS_COPY_LANES")) ctx->copy_lanes = (uint32_t)strtoul(v, nullptr, 0);
     uint32_t per_sm = 128;
     if (const char *v = getenv("GLS_SIM_WARP_SEGS")) per_sm = std::max(1u, (uint32_t)strtoul(v, nullptr, 0));
@@ -264,6 +267,8 @@ extern "C" int gls_destroy(gls_ctx *ctx)
         if (ctx->side[c]) cudaStreamDestroy(ctx->side[c]);
         if (ctx->side_prio[c]) cudaStreamDestroy(ctx->side_prio[c]);
         if (ctx->join_ev[c]) cudaEventDestroy(ctx->join_ev[c]);
+        if (ctx->link_ev[c]) cudaEventDestroy(ctx->link_ev[c]);
+        if (ctx->copy_ev[c]) cudaEventDestroy(ctx->copy_ev[c]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
     delete ctx;
@@ -704,7 +709,8 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
     return GLS_OK;
 }
 
-static WinDev make_windev(gls_ctx *ctx, Window *w, const LevelScratch &ls)
+// parity 1: the per-gate-output tables of odd levels
+static WinDev make_windev(gls_ctx *ctx, Window *w, const LevelScratch &ls, int parity = 0)
 {
     WinDev d;
     std::memset(&d, 0, sizeof d);
@@ -718,13 +724,13 @@ static WinDev make_windev(gls_ctx *ctx, Window *w, const LevelScratch &ls)
     d.err = reinterpret_cast<uint32_t *>(sm + 5);
     d.n_segs = reinterpret_cast<uint32_t *>(sm + 6);
     d.n_over = sm + 7;
-    d.res = ls.res.as<uint32_t>();
+    d.res = (parity ? ls.res1 : ls.res).as<uint32_t>();
     d.pred = ls.pred.as<uint32_t>();
     d.stim_nets = w->stim_dev.as<uint32_t>();
     d.n_stim = (uint32_t)w->stim_nets.size();
-    d.seg_base = ls.seg_base.as<uint32_t>();
-    d.slot = ls.slot.as<uint64_t>();
-    d.scr = ls.scr.as<uint64_t>();
+    d.seg_base = (parity ? ls.seg_base1 : ls.seg_base).as<uint32_t>();
+    d.slot = (parity ? ls.slot1 : ls.slot).as<uint64_t>();
+    d.scr = (parity ? ls.scr1 : ls.scr).as<uint64_t>();
     d.segs = ls.segs.as<SegRec>();
     d.copies = ls.copies.as<CopyRec>();
     d.scratch = ls.scratch.as<uint32_t>();
@@ -766,15 +772,16 @@ static int reset_window(gls_ctx *ctx, Window *w)
     return GLS_OK;
 }
 
-// The launches of a run of nwin windows (device array dw): stimulus SAIF,
-// then per level the presize (learned mode), plan, simulate per fan-in
-// class, link and copy.  With `prof` the kernel classes are bracketed with
-// events (not during stream capture).
-static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint32_t nwin, uint32_t max_stim,
-                          bool prof, uint32_t *launches)
+// The launches of a run of nwin windows: stimulus SAIF, then per level the
+// presize (learned mode), plan, simulate per fan-in class, link and copy.
+// dw[p] / h[p] are the descriptors (device array / window 0 on the host)
+// whose per-gate-output tables serve levels of parity p.  With `prof` the
+// kernel classes are bracketed with events (not during stream capture).
+static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev *const h[2], uint32_t nwin,
+                          uint32_t max_stim, bool prof, uint32_t *launches)
 {
     if (prof) prof_mark(ctx);
-    launch_stim_saif(dw, h0, nwin, max_stim, ctx->stream);
+    launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stream);
     ++*launches;
     if (prof) prof_mark(ctx);
     LevelArgs a;
@@ -786,38 +793,62 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
         CK(ctx->wave_e.ensure(nlev * kClasses * 8 + 8), "alloc wave totals");
         CK(cudaMemsetAsync(ctx->wave_e.p, 0, nlev * kClasses * 8, ctx->stream), "clear wave totals");
     }
+    // Overlapped levels: every class runs simulate, link and copy on its own
+    // stream; the main stream plans the next level as soon as every class
+    // has linked (the plan needs the new lists' lengths and places, and
+    // writes the other set of per-gate-output tables), while the copies
+    // still run; a class's next simulation waits for every class's copy.
+    // Not in learned mode: the presize reads SAIF counts that the copies add.
+    const bool overlap_ok = ctx->concurrent && ctx->pipeline && ctx->plan_overlap && !(prof && ctx->opts.profile) &&
+                            a.alloc_mode != kAllocLearned;
+    bool copied[kClasses] = {false, false, false, false};   // the class copied at the previous level
     for (size_t L = 0; L < nlev; ++L) {
         a.lo = ctx->drv_level_start[L];
         a.hi = ctx->drv_level_start[L + 1];
         if (a.hi == a.lo) continue;
+        const WinDev *dwL = dw[L & 1];
+        const WinDev &hL = *h[L & 1];
         a.wave_e = nwin > 1 ? ctx->wave_e.as<unsigned long long>() + L * kClasses : nullptr;
         if (nwin > 1) {
-            launch_wave_events(dw, nwin, a, ctx->stream);
+            launch_wave_events(dwL, nwin, a, ctx->stream);
             ++*launches;
         }
         if (a.alloc_mode == kAllocLearned) {
             // the level's presize predictions (tensor cores) before its slots are planned
             PresizeArgs pa;
             ctx_presize_args(ctx, &pa);
-            pa.wv = dw;
+            pa.wv = dwL;
             pa.nwin = nwin;
             pa.lo = a.lo;
             pa.n = a.hi - a.lo;
             launch_presize(pa, true, ctx->stream);
             ++*launches;
         }
-        launch_plan(dw, h0, nwin, a, ctx->stream);
+        launch_plan(dwL, hL, nwin, a, ctx->stream);
         if (prof) prof_mark(ctx);
         int n_cls = 0;
         for (int c = 0; c < kClasses; ++c)
             n_cls += ctx->cls_start[(kClasses + 1) * L + c + 1] > ctx->cls_start[(kClasses + 1) * L + c];
+        const bool overlap = overlap_ok && n_cls > 0;
         // Concurrent: the fan-in classes simulate on their own streams, so
         // one class's blocks fill another's tail (linking and copying every
         // class together after the join measured faster than per class).
         // Profiled runs keep the classes apart.
-        const bool fork = ctx->concurrent && !(prof && ctx->opts.profile) && n_cls > 1;
+        const bool fork = overlap || (ctx->concurrent && !(prof && ctx->opts.profile) && n_cls > 1);
         if (fork) CK(cudaEventRecord(ctx->fork_ev, ctx->stream), "fork");
+        if (overlap) {
+            // every class stream waits for the plan and for every class's
+            // copy of the previous level, before any class records anew
+            for (int c = 0; c < kClasses; ++c) {
+                if (ctx->cls_start[(kClasses + 1) * L + c + 1] <= ctx->cls_start[(kClasses + 1) * L + c]) continue;
+                cudaStream_t st = ctx->class_priority ? ctx->side_prio[c] : ctx->side[c];
+                CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
+                for (int c2 = 0; c2 < kClasses; ++c2)
+                    if (copied[c2]) CK(cudaStreamWaitEvent(st, ctx->copy_ev[c2], 0), "copy wait");
+            }
+        }
         bool first = true;
+        bool linked[kClasses] = {false, false, false, false};
         for (int ci = 0; ci < kClasses; ++ci) {
             // wider gates first when the classes run together: they carry
             // the most events per gate, so their chain sets the level's length
@@ -825,33 +856,54 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *dw, const WinDev &h0, uint
             const uint32_t d0 = ctx->cls_start[(kClasses + 1) * L + c], d1 = ctx->cls_start[(kClasses + 1) * L + c + 1];
             if (d1 <= d0) continue;
             // the first class on the main stream, the others beside it
+            // (overlapped: every class beside it)
             cudaStream_t st = ctx->stream;
-            if (fork && (!first || ctx->class_priority)) {
+            if (overlap) {
+                st = ctx->class_priority ? ctx->side_prio[c] : ctx->side[c];
+            } else if (fork && (!first || ctx->class_priority)) {
                 st = ctx->class_priority ? ctx->side_prio[c] : ctx->side[c];
                 CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
             }
-            launch_sim(dw, h0, nwin, a, c, d0, d1, ctx->sm_count, st);
+            launch_sim(dwL, hL, nwin, a, c, d0, d1, ctx->sm_count, st);
             ++*launches;
             if (fork && ctx->pipeline) {   // the class's link and copy right behind it
-                launch_link(dw, h0, nwin, a, d0, d1, st);
-                launch_copy(dw, h0, nwin, a, d0, d1, ctx->sm_count, st);
+                launch_link(dwL, hL, nwin, a, d0, d1, st);
+                if (overlap) {
+                    CK(cudaEventRecord(ctx->link_ev[c], st), "link done");
+                    linked[c] = true;
+                }
+                launch_copy(dwL, hL, nwin, a, d0, d1, ctx->sm_count, st);
+                if (overlap) CK(cudaEventRecord(ctx->copy_ev[c], st), "copy done");
                 *launches += 2;
             }
-            if (st != ctx->stream) {
+            if (st != ctx->stream && !overlap) {
                 CK(cudaEventRecord(ctx->join_ev[c], st), "join");
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[c], 0), "join wait");
             }
             first = false;
         }
+        if (overlap) {
+            // the next plan waits for the links only
+            for (int c = 0; c < kClasses; ++c) {
+                if (linked[c]) CK(cudaStreamWaitEvent(ctx->stream, ctx->link_ev[c], 0), "link wait");
+                copied[c] = linked[c];
+            }
+        } else {
+            // this level's kernels are all on or joined to the main stream
+            for (int c = 0; c < kClasses; ++c) copied[c] = false;
+        }
         if (prof) prof_mark(ctx);
         if (!(fork && ctx->pipeline)) {
-            launch_link(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->stream);
-            launch_copy(dw, h0, nwin, a, 0, a.hi - a.lo, ctx->sm_count, ctx->stream);
+            launch_link(dwL, hL, nwin, a, 0, a.hi - a.lo, ctx->stream);
+            launch_copy(dwL, hL, nwin, a, 0, a.hi - a.lo, ctx->sm_count, ctx->stream);
             *launches += 2;
         }
         if (prof) prof_mark(ctx);
         ++*launches;   // the plan
     }
+    // the last level's copies join the main stream
+    for (int c = 0; c < kClasses; ++c)
+        if (copied[c]) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[c], 0), "final join");
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;
 }
@@ -863,10 +915,12 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     w->saif_only = false;
     rc = reset_window(ctx, w);
     if (rc) return rc;
-    const WinDev d = make_windev(ctx, w, *ctx->lsc[0]);
-    CK(w->dwin.ensure(sizeof(WinDev)), "alloc window descriptor");
-    CK(cudaMemcpyAsync(w->dwin.p, &d, sizeof d, cudaMemcpyHostToDevice, ctx->stream), "upload window descriptor");
-    return enqueue_levels(ctx, w->dwin.as<WinDev>(), d, 1, d.n_stim, true, launches);
+    const WinDev d[2] = {make_windev(ctx, w, *ctx->lsc[0], 0), make_windev(ctx, w, *ctx->lsc[0], 1)};
+    CK(w->dwin.ensure(sizeof d), "alloc window descriptor");
+    CK(cudaMemcpyAsync(w->dwin.p, d, sizeof d, cudaMemcpyHostToDevice, ctx->stream), "upload window descriptor");
+    const WinDev *dw[2] = {w->dwin.as<WinDev>(), w->dwin.as<WinDev>() + 1};
+    const WinDev *hp[2] = {&d[0], &d[1]};
+    return enqueue_levels(ctx, dw, hp, 1, d[0].n_stim, true, launches);
 }
 
 // Totals of a run over its windows.
@@ -1038,8 +1092,9 @@ static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
     while (ctx->lsc.size() < b) ctx->lsc.push_back(new LevelScratch);
     for (uint64_t k = 0; k < b; ++k)
         CK(ctx->lsc[k]->ensure(ctx->max_width, ctx->seg_cap, ctx->scr_cap), "alloc level work spaces");
-    if (!ctx->hwave.ensure(kMaxWave * sizeof(WinDev))) return fail(ctx, GLS_ENOMEM, "pinned wave descriptors");
-    CK(ctx->dwave.ensure(kMaxWave * sizeof(WinDev)), "alloc wave descriptors");
+    // two descriptor sets: the per-gate-output tables of even and odd levels
+    if (!ctx->hwave.ensure(2 * kMaxWave * sizeof(WinDev))) return fail(ctx, GLS_ENOMEM, "pinned wave descriptors");
+    CK(ctx->dwave.ensure(2 * kMaxWave * sizeof(WinDev)), "alloc wave descriptors");
     // allocated here, never inside a stream capture
     CK(ctx->wave_e.ensure((ctx->drv_level_start.size() - 1) * kClasses * 8 + 8), "alloc wave totals");
     *B = b;
@@ -1062,13 +1117,17 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         if (rc == GLS_OK) rc = reset_window(ctx, w);
         if (rc) return rc;
         w->saif_only = false;
-        hw[k] = make_windev(ctx, w, *ctx->lsc[k]);
+        hw[k] = make_windev(ctx, w, *ctx->lsc[k], 0);
+        hw[kMaxWave + k] = make_windev(ctx, w, *ctx->lsc[k], 1);
         max_stim = std::max(max_stim, hw[k].n_stim);
     }
     CK(cudaEventRecord(e0, ctx->stream), "event");
-    CK(cudaMemcpyAsync(ctx->dwave.p, hw, nwin * sizeof(WinDev), cudaMemcpyHostToDevice, ctx->stream),
-       "upload wave descriptors");
-    const WinDev *dw = ctx->dwave.as<WinDev>();
+    for (int p = 0; p < 2; ++p)
+        CK(cudaMemcpyAsync(ctx->dwave.as<WinDev>() + p * kMaxWave, hw + p * kMaxWave, nwin * sizeof(WinDev),
+                           cudaMemcpyHostToDevice, ctx->stream),
+           "upload wave descriptors");
+    const WinDev *dw[2] = {ctx->dwave.as<WinDev>(), ctx->dwave.as<WinDev>() + kMaxWave};
+    const WinDev *hp[2] = {&hw[0], &hw[kMaxWave]};
     if (o.use_graph && nwin > 1) {
         // one graph per wave shape; the descriptors it reads are rewritten per wave
         gls_ctx::WaveGraph key{nwin, max_stim, ctx->warp_mask, (uint32_t)ctx->opts.alloc_mode, ctx->seg_per_sm,
@@ -1085,7 +1144,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
             cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
             int rc = GLS_OK;
             if (e == cudaSuccess) {
-                rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &l);
+                rc = enqueue_levels(ctx, dw, hp, nwin, max_stim, false, &l);
                 const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
                 if (rc == GLS_OK && e2 != cudaSuccess) e = e2;
             }
@@ -1100,7 +1159,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         CK(cudaGraphLaunch(ge, ctx->stream), "graph launch");
         acc.launches += l;
     } else {
-        int rc = enqueue_levels(ctx, dw, hw[0], nwin, max_stim, false, &acc.launches);
+        int rc = enqueue_levels(ctx, dw, hp, nwin, max_stim, false, &acc.launches);
         if (rc) return rc;
     }
     CK(cudaEventRecord(e1, ctx->stream), "event");

@@ -137,6 +137,9 @@ struct PinBuf {   // page-locked host staging, reused across windows
 // together takes one set per window.
 struct LevelScratch {
     DevBuf seg_base, slot, scr, res, pred, segs, copies, scratch;
+    // the per-gate-output tables of odd levels: the next level's plan fills
+    // one set while the previous level's copy still reads the other
+    DevBuf seg_base1, slot1, scr1, res1;
     uint32_t seg_cap = 0;
     uint64_t scr_cap = 0;
     uint32_t width = 0;
@@ -150,6 +153,10 @@ struct LevelScratch {
             if (e == cudaSuccess) e = scr.ensure(n * 8);
             if (e == cudaSuccess) e = res.ensure(n * 4);
             if (e == cudaSuccess) e = pred.ensure(n * 4);
+            if (e == cudaSuccess) e = seg_base1.ensure(n * 4);
+            if (e == cudaSuccess) e = slot1.ensure(n * 8);
+            if (e == cudaSuccess) e = scr1.ensure(n * 8);
+            if (e == cudaSuccess) e = res1.ensure(n * 4);
             if (e == cudaSuccess) width = w;
         }
         if (e == cudaSuccess && segs_need > seg_cap) {
@@ -165,7 +172,8 @@ struct LevelScratch {
     }
     void release()
     {
-        DevBuf *all[] = {&seg_base, &slot, &scr, &res, &pred, &segs, &copies, &scratch};
+        DevBuf *all[] = {&seg_base, &slot, &scr, &res, &pred, &segs, &copies, &scratch,
+                         &seg_base1, &slot1, &scr1, &res1};
         for (DevBuf *b : all) b->release();
         seg_cap = 0;
         scr_cap = 0;
@@ -201,6 +209,8 @@ struct gls_ctx {
     cudaStream_t side[gls::kClasses] = {};
     cudaStream_t side_prio[gls::kClasses] = {};   // the same with priority rising with fan-in
     cudaEvent_t fork_ev = nullptr, join_ev[gls::kClasses] = {};
+    cudaEvent_t link_ev[gls::kClasses] = {}, copy_ev[gls::kClasses] = {};
+    bool plan_overlap = true;        // the next level's plan runs beside this level's copies (GLS_PLAN_OVERLAP)
     bool concurrent = true;
     bool wide_first = false;         // launch the widest fan-in class first (GLS_WIDE_FIRST)
     bool class_priority = false;     // wider classes on higher-priority side streams (GLS_CLASS_PRIORITY)

@@ -80,14 +80,15 @@ def test_gpu_pool_offsets_past_2_34_events(gpu, oracle_bin):
         assert_same(gw, gs, ow, osaif, f"gap seg {seg} mask {mask}")
 
 
-@pytest.mark.parametrize("knobs", [{"GLS_SIM_CONCURRENT": "0"}, {"GLS_SIM_PIPELINE": "0"},
+@pytest.mark.parametrize("knobs", [{"GLS_SIM_CONCURRENT": "0"}, {"GLS_SIM_PIPELINE": "0"}, {"GLS_PLAN_OVERLAP": "0"},
                                    {"GLS_COPY_LANES": "4"}, {"GLS_COPY_LANES": "16"}, {"GLS_COPY_LANES": "32"},
                                    {"profile": True}, {"schedule": (512, 7, 0)}, {"schedule": (8192, 1, 1)},
                                    {"schedule": (2048, 0, 1)}])
 def test_gpu_schedules_and_streams_agree(knobs, gpu, oracle_bin):
     """Results never depend on how a level is scheduled: fan-in classes in
-    turn or concurrently, link and copy per class or per level, lanes per
-    copied segment, profiled runs, segments per SM, warp-per-segment classes."""
+    turn or concurrently, link and copy per class or per level, the next
+    level's plan beside the copies or after them, lanes per copied segment,
+    profiled runs, segments per SM, warp-per-segment classes."""
     nl, st = random_case(960, max_gates=120, max_in=8, horizon=20000, max_events=2000)
     ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
     env = {k: v for k, v in knobs.items() if k.startswith("GLS_")}
