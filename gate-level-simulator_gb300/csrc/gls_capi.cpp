@@ -139,7 +139,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         delete ctx;
         return GLS_ECUDA;
     }
-    ctx->def_delay = (uint32_t)(uint64_t)(1.0 * ctx->opts.delay_factor);
+    ctx->def_delay = (uint32_t)std::min<uint64_t>((uint64_t)(1.0 * ctx->opts.delay_factor), kMaxDelay);
     // tuning knobs: which fan-in classes (bit 0: one input net, 1: two,
     // 2: three) run warp-per-segment, and how many segments per SM those
     // classes are cut into
@@ -369,8 +369,8 @@ extern "C" int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl)
                         return fail(ctx, GLS_ERANGE, "instance %u: delay out of range", i);
                     ArcDev ad;
                     ad.info = (uint32_t)A.edge | (slotp << 2);
-                    ad.rise = (uint32_t)(uint64_t)r;
-                    ad.fall = (uint32_t)(uint64_t)f;
+                    ad.rise = (uint32_t)std::min<uint64_t>((uint64_t)r, kMaxDelay);
+                    ad.fall = (uint32_t)std::min<uint64_t>((uint64_t)f, kMaxDelay);
                     ad.pad = 0;
                     h_arcs.push_back(ad);
                     ++na;

@@ -92,6 +92,21 @@ __host__ __device__ constexpr uint32_t neg_table()
     return t;
 }
 constexpr uint64_t kSenseTab = sense_table();
+// 2 bits per (pre * 4 + cur), pre != cur: the sense minus one (a change
+// always has sense 1..4; entries with pre == cur are 0 and never read)
+__host__ __device__ constexpr uint32_t sense1_table()
+{
+    uint32_t t = 0;
+    for (uint32_t k = 0; k < 16; ++k)
+        if ((k >> 2) != (k & 3u)) t |= (uint32_t)(sense_of(k >> 2, k & 3u) - 1) << (2 * k);
+    return t;
+}
+constexpr uint32_t kSense1Tab = sense1_table();
+static_assert(sense_of(kV0, kVX) == 1 && sense_of(kVX, kV0) == 2 && sense_of(kVX, kVZ) == 3 && sense_of(kVZ, kVX) == 4,
+              "sense classes");
+// delays are stored capped at kMaxTime + 1: an output time past kMaxTime is
+// an error whichever arc gives it, and t + d then never wraps 32 bits
+constexpr uint32_t kMaxDelay = kMaxTime + 1;
 constexpr uint32_t kNegTab = neg_table();
 
 struct SegRec {             // one time segment of one gate output

@@ -100,15 +100,15 @@ __device__ uint32_t select_delay(const ArcDev *__restrict__ arcs, int n_arcs, ui
 // one negedge arc: then a single changed net selects exactly one arc (or
 // none), and several changed nets take the minimum over their arcs.
 template <int M>
-__device__ __forceinline__ uint32_t regular_delay(const NetDelay *__restrict__ nd, uint32_t chg, int so,
+__device__ __forceinline__ uint32_t regular_delay(const NetDelay *__restrict__ nd, uint32_t chg, uint32_t so1,
                                                   uint32_t curp, uint32_t lastp, uint32_t defd)
 {
-    uint32_t d = kInf;
+    uint32_t d = kInf;   // so1: the output sense minus one
 #pragma unroll
     for (int j = 0; j < M; ++j) {
         if ((chg >> j) & 1u) {
             const uint32_t neg = (kNegTab >> (slot_val(lastp, j) * 4 + slot_val(curp, j))) & 1u;
-            d = min(d, __ldg(&nd[j].d[neg * 4 + so - 1]));
+            d = min(d, __ldg(&nd[j].d[neg * 4 + so1]));
         }
     }
     return d == kInf ? defd : d;
@@ -623,13 +623,14 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
         }
         const uint32_t F = kSlut ? slut_get<M>(sl, curp) : lut[lut_index(curp, md)];
         if (F == fprev) continue;
-        const int so = (int)((kSenseTab >> (3 * (fprev * 4 + F))) & 7u);
+        const uint32_t so1 = (kSense1Tab >> (2 * (fprev * 4 + F))) & 3u;   // F != fprev: sense 1..4, minus one
         fprev = F;
         const uint32_t t = ev_time(mk);
-        const uint32_t d = regular ? regular_delay<M>(nd, chg, so, curp, lastp, a.def_delay)
-                                   : select_delay(a.arcs + md.arc_off, md.n_arcs, chg, so, curp, lastp, a.def_delay);
-        const uint32_t o = t + d;
-        if (o > kMaxTime || o < t) { atomicOr(w.err, kErrTime); break; }
+        const uint32_t d = regular ? regular_delay<M>(nd, chg, so1, curp, lastp, a.def_delay)
+                                   : select_delay(a.arcs + md.arc_off, md.n_arcs, chg, (int)so1 + 1, curp, lastp,
+                                                  a.def_delay);
+        const uint32_t o = t + d;   // delays are at most kMaxDelay: the sum does not wrap
+        if (o > kMaxTime) { atomicOr(w.err, kErrTime); break; }
         min_o = min(min_o, o);
         // inertial update, src/simulate.cpp:991-1009
         while (cnt > 0 && ev_time(top) >= o) {
