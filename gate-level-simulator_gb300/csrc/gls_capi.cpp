@@ -133,6 +133,9 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->copy_ev[c], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stim_side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stim_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stim_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e != cudaSuccess) {
@@ -271,6 +274,9 @@ extern "C" int gls_destroy(gls_ctx *ctx)
         if (ctx->copy_ev[c]) cudaEventDestroy(ctx->copy_ev[c]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->stim_side) cudaStreamDestroy(ctx->stim_side);
+    if (ctx->stim_fork) cudaEventDestroy(ctx->stim_fork);
+    if (ctx->stim_join) cudaEventDestroy(ctx->stim_join);
     delete ctx;
     return GLS_OK;
 }
@@ -780,19 +786,8 @@ static int reset_window(gls_ctx *ctx, Window *w)
 static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev *const h[2], uint32_t nwin,
                           uint32_t max_stim, bool prof, uint32_t *launches)
 {
-    if (prof) prof_mark(ctx);
-    launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stream);
-    ++*launches;
-    if (prof) prof_mark(ctx);
     LevelArgs a;
     ctx_level_args(ctx, &a);
-    const size_t nlev = ctx->drv_level_start.size() - 1;
-    if (nwin > 1) {
-        // per level, the wave's fan-in events per class: segments are cut to
-        // one size across the windows of the wave
-        CK(ctx->wave_e.ensure(nlev * kClasses * 8 + 8), "alloc wave totals");
-        CK(cudaMemsetAsync(ctx->wave_e.p, 0, nlev * kClasses * 8, ctx->stream), "clear wave totals");
-    }
     // Overlapped levels: every class runs simulate, link and copy on its own
     // stream; the main stream plans the next level as soon as every class
     // has linked (the plan needs the new lists' lengths and places, and
@@ -801,6 +796,26 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
     // Not in learned mode: the presize reads SAIF counts that the copies add.
     const bool overlap_ok = ctx->concurrent && ctx->pipeline && ctx->plan_overlap && !(prof && ctx->opts.profile) &&
                             a.alloc_mode != kAllocLearned;
+    if (prof) prof_mark(ctx);
+    if (overlap_ok) {
+        // the stimulus nets' SAIF beside the levels (nothing else reads or
+        // writes their counts; learned mode's presize would read them)
+        CK(cudaEventRecord(ctx->stim_fork, ctx->stream), "stim fork");
+        CK(cudaStreamWaitEvent(ctx->stim_side, ctx->stim_fork, 0), "stim fork wait");
+        launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stim_side);
+        CK(cudaEventRecord(ctx->stim_join, ctx->stim_side), "stim join");
+    } else {
+        launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stream);
+    }
+    ++*launches;
+    if (prof) prof_mark(ctx);
+    const size_t nlev = ctx->drv_level_start.size() - 1;
+    if (nwin > 1) {
+        // per level, the wave's fan-in events per class: segments are cut to
+        // one size across the windows of the wave
+        CK(ctx->wave_e.ensure(nlev * kClasses * 8 + 8), "alloc wave totals");
+        CK(cudaMemsetAsync(ctx->wave_e.p, 0, nlev * kClasses * 8, ctx->stream), "clear wave totals");
+    }
     bool copied[kClasses] = {false, false, false, false};   // the class copied at the previous level
     for (size_t L = 0; L < nlev; ++L) {
         a.lo = ctx->drv_level_start[L];
@@ -901,9 +916,10 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
         if (prof) prof_mark(ctx);
         ++*launches;   // the plan
     }
-    // the last level's copies join the main stream
+    // the last level's copies and the stimulus SAIF join the main stream
     for (int c = 0; c < kClasses; ++c)
         if (copied[c]) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[c], 0), "final join");
+    if (overlap_ok) CK(cudaStreamWaitEvent(ctx->stream, ctx->stim_join, 0), "stim join wait");
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;
 }

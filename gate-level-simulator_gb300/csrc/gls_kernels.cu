@@ -1468,7 +1468,10 @@ constexpr int kCopyUnroll = GLS_COPY_UNROLL;   // entries per lane loaded ahead 
 // output's counters.  The next segment's record is loaded while the current
 // one is copied.
 template <bool kBatch, int W>
-__global__ void __launch_bounds__(256) k_copy(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
+#ifndef GLS_COPY_BLOCKS
+#define GLS_COPY_BLOCKS 5   // resident blocks per SM the copy kernel is compiled for (48 registers)
+#endif
+__global__ void __launch_bounds__(256, GLS_COPY_BLOCKS) k_copy(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     const unsigned FULL = 0xffffffffu;
     __shared__ uint32_t s_pre[kBatch ? kMaxWave + 1 : 2];
