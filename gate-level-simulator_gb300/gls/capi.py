@@ -29,7 +29,7 @@ EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
             "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched",
-            "gls_autotune", "gls_set_schedule"]
+            "gls_autotune", "gls_set_schedule", "gls_levelize"]
 
 
 class GlsError(RuntimeError):
@@ -133,6 +133,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_run_batched.argtypes = [C.c_void_p, C.POINTER(BatchOpts)]
     lib.gls_autotune.argtypes = [C.c_void_p, C.POINTER(BatchOpts), C.POINTER(TuneResult)]
     lib.gls_set_schedule.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
+    lib.gls_levelize.argtypes = [C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
     lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -170,6 +171,40 @@ def cell_lut(cell_rec: np.ndarray, prims: np.ndarray, out: int, calc_mode: int) 
     if rc:
         raise GlsError(rc, "gls_cell_lut")
     return lut
+
+
+def levelize_gpu(pred_start: np.ndarray, pred: np.ndarray, device: int = 0):
+    """Kahn levels on the GPU (gls_levelize): pred_start[n + 1] / pred[] list
+    every instance's predecessor instances.  Returns (order, level_start):
+    the instances level by level in instance order, and every level's first
+    position followed by n.  Raises GlsError on a combinational loop."""
+    lib = load_library()
+    ps = np.ascontiguousarray(pred_start, np.uint64)
+    pr = np.ascontiguousarray(pred, np.uint32)
+    n = len(ps) - 1
+    order = np.zeros(max(n, 1), np.uint32)
+    level_start = np.zeros(n + 1, np.uint32)
+    nl = C.c_uint32(0)
+    rc = lib.gls_levelize(device, n, _ptr(ps), _ptr(pr) if len(pr) else None, _ptr(order), _ptr(level_start),
+                          C.byref(nl))
+    if rc:
+        raise GlsError(rc, "gls_levelize: malformed predecessor table or combinational loop")
+    return order[:n], level_start[: nl.value + 1]
+
+
+def netlist_preds(in_nets: list[list[int]], out_nets: list[list[int]]):
+    """Predecessor table of an instance list: the instances driving each
+    instance's input nets (the edges of src/process.cpp:90-114)."""
+    driver: dict[int, int] = {}
+    for i, outs in enumerate(out_nets):
+        for net in outs:
+            driver[net] = i
+    starts, preds = [0], []
+    for ins in in_nets:
+        ps = sorted({driver[n] for n in ins if n in driver})
+        preds.extend(ps)
+        starts.append(len(preds))
+    return np.array(starts, np.uint64), np.array(preds, np.uint32)
 
 
 class Simulator:

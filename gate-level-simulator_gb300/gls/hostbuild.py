@@ -22,8 +22,7 @@ def _build_tool(name: str, srcs: list[str], force: bool) -> Path:
         return out
     cmd = ["g++", "-std=c++17", "-O2", f"-I{REPO / 'include'}", f"-I{HOST}", *map(str, (HOST / s for s in srcs)),
            "-o", str(out), "-pthread"]
-    if name == "gls_simulate":
-        cmd += [f"-L{LIB_DIR}", "-lgls", "-Wl,-rpath,$ORIGIN/../lib"]
+    cmd += [f"-L{LIB_DIR}", "-lgls", "-Wl,-rpath,$ORIGIN/../lib"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError(f"building {name} failed:\n{r.stdout}\n{r.stderr}")

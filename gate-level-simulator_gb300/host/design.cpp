@@ -629,7 +629,7 @@ bool parse_sdf(const std::string &text, Design &d, const Library &lib, std::stri
 // an edge runs from an instance to every instance reading one of its
 // output nets; each level takes, in instance order, every instance whose
 // predecessors are all placed.  Reads through assign aliases count.
-bool levelize(Design &d, std::string *err)
+void instance_preds(const Design &d, std::vector<uint64_t> &start, std::vector<uint32_t> &pred)
 {
     const size_t n = d.insts.size();
     std::vector<uint32_t> alias_to(d.net_names.size());
@@ -644,38 +644,68 @@ bool levelize(Design &d, std::string *err)
         const Cell &c = d.cells[d.insts[i].cell];
         for (size_t o = 0; o < c.outputs.size(); ++o) driver[d.insts[i].pins[c.inputs.size() + o]] = (int)i;
     }
-    std::vector<std::vector<uint32_t>> succ(n);
-    std::vector<int> indeg(n, 0);
+    start.assign(1, 0);
+    pred.clear();
+    std::vector<uint32_t> ps;
     for (size_t i = 0; i < n; ++i) {
         const Cell &c = d.cells[d.insts[i].cell];
-        std::set<int> preds;
+        ps.clear();
         for (size_t p = 0; p < c.inputs.size(); ++p) {
             const int drv = driver[resolve(d.insts[i].pins[p])];
-            if (drv >= 0) preds.insert(drv);
+            if (drv >= 0) ps.push_back((uint32_t)drv);
         }
-        for (int p : preds) succ[p].push_back((uint32_t)i);
-        indeg[i] = (int)preds.size();
+        std::sort(ps.begin(), ps.end());
+        ps.erase(std::unique(ps.begin(), ps.end()), ps.end());
+        pred.insert(pred.end(), ps.begin(), ps.end());
+        start.push_back(pred.size());
     }
-    std::vector<uint32_t> order;
-    d.level_start.assign(1, 0);
-    while (order.size() < n) {
-        std::vector<uint32_t> q;
-        for (size_t i = 0; i < n; ++i)
-            if (indeg[i] == 0) q.push_back((uint32_t)i);
-        if (q.empty()) {
-            if (err) *err = "combinational loop: the netlist cannot be levelized";
-            return false;
-        }
-        for (uint32_t i : q) indeg[i] = -1;
-        for (uint32_t i : q)
-            for (uint32_t j : succ[i]) --indeg[j];
-        order.insert(order.end(), q.begin(), q.end());
-        d.level_start.push_back((uint32_t)order.size());
-    }
+}
+
+void apply_levels(Design &d, const std::vector<uint32_t> &order, const std::vector<uint32_t> &level_start)
+{
     std::vector<Instance> sorted;
-    sorted.reserve(n);
+    sorted.reserve(order.size());
     for (uint32_t i : order) sorted.push_back(std::move(d.insts[i]));
     d.insts = std::move(sorted);
+    d.level_start = level_start;
+}
+
+bool levelize(Design &d, std::string *err)
+{
+    const size_t n = d.insts.size();
+    std::vector<uint64_t> start;
+    std::vector<uint32_t> pred;
+    instance_preds(d, start, pred);
+    // successors and in-degrees, then one frontier per level
+    std::vector<uint64_t> sstart(n + 1, 0);
+    for (uint32_t p : pred) ++sstart[p + 1];
+    for (size_t i = 0; i < n; ++i) sstart[i + 1] += sstart[i];
+    std::vector<uint32_t> succ(pred.size());
+    std::vector<uint64_t> fill(sstart.begin(), sstart.end() - 1);
+    std::vector<uint32_t> indeg(n);
+    for (size_t i = 0; i < n; ++i) {
+        indeg[i] = (uint32_t)(start[i + 1] - start[i]);
+        for (uint64_t e = start[i]; e < start[i + 1]; ++e) succ[fill[pred[e]]++] = (uint32_t)i;
+    }
+    std::vector<uint32_t> order, level_start(1, 0), q;
+    order.reserve(n);
+    for (size_t i = 0; i < n; ++i)
+        if (indeg[i] == 0) q.push_back((uint32_t)i);
+    while (!q.empty()) {
+        order.insert(order.end(), q.begin(), q.end());
+        level_start.push_back((uint32_t)order.size());
+        std::vector<uint32_t> next;
+        for (uint32_t i : q)
+            for (uint64_t e = sstart[i]; e < sstart[i + 1]; ++e)
+                if (--indeg[succ[e]] == 0) next.push_back(succ[e]);
+        std::sort(next.begin(), next.end());   // a level in instance order
+        q.swap(next);
+    }
+    if (order.size() < n) {
+        if (err) *err = "combinational loop: the netlist cannot be levelized";
+        return false;
+    }
+    apply_levels(d, order, level_start);
     return true;
 }
 

@@ -73,6 +73,12 @@ bool parse_vlib(const std::string &text, Library &lib, std::string *err);
 bool parse_gv(const std::string &text, const Library &lib, Design &d, std::string *err);
 bool parse_sdf(const std::string &text, Design &d, const Library &lib, std::string *err);
 bool levelize(Design &d, std::string *err);
+// The levelization in two halves, for a levelizer elsewhere (gls_levelize on
+// the GPU): every instance's distinct predecessors (the instances driving
+// its input nets, through assign aliases), and the reordering of the
+// instances by level.
+void instance_preds(const Design &d, std::vector<uint64_t> &start, std::vector<uint32_t> &pred);
+void apply_levels(Design &d, const std::vector<uint32_t> &order, const std::vector<uint32_t> &level_start);
 bool write_inter(const std::string &path, const Design &d, std::string *err);
 bool read_inter(const std::string &path, Design &d, std::string *err);
 

@@ -1,15 +1,20 @@
-// gls_process <vlib> <gv> <sdf> <inter.dat>
+// gls_process [--gpu-levelize] <vlib> <gv> <sdf> <inter.dat>
 //
 // The `process` step of the reference (src/process.cpp:178-610): read the
 // Verilog cell library, the flat gate-level netlist and the SDF file,
 // levelize the instance graph and write the levelized design to inter.dat
-// (native binary format; see host/design.cpp).
+// (native binary format; see host/design.cpp).  With --gpu-levelize the
+// levels are computed on GPU 0 (gls_levelize); the file is the same.
 #include <cstdio>
 #include <string>
+#include <vector>
 #include "design.h"
+#include "gls.h"
 
 int main(int argc, char **argv)
 {
+    const bool gpu = argc == 6 && std::string(argv[1]) == "--gpu-levelize";
+    if (gpu) ++argv, --argc;
     if (argc != 5) {
         printf("[USAGE] ./gls_process vlib_path gv_path sdf_path intermediate_file\n");
         return 255;
@@ -36,7 +41,26 @@ int main(int argc, char **argv)
         return 255;
     }
     printf("INFO: SDF file's parsing done!\n");
-    if (!levelize(d, &err)) {
+    if (gpu) {
+        std::vector<uint64_t> start;
+        std::vector<uint32_t> pred;
+        instance_preds(d, start, pred);
+        const uint32_t n = (uint32_t)d.insts.size();
+        std::vector<uint32_t> order(n ? n : 1), level_start(n + 1);
+        uint32_t n_levels = 0;
+        const int rc = gls_levelize(0, n, start.data(), pred.data(), order.data(), level_start.data(), &n_levels);
+        if (rc == GLS_EINVAL) {
+            printf("ERROR: combinational loop: the netlist cannot be levelized\n");
+            return 255;
+        }
+        if (rc) {
+            printf("ERROR: GPU levelization failed (code %d)\n", rc);
+            return 255;
+        }
+        order.resize(n);
+        level_start.resize(n_levels + 1);
+        apply_levels(d, order, level_start);
+    } else if (!levelize(d, &err)) {
         printf("ERROR: %s\n", err.c_str());
         return 255;
     }

@@ -235,6 +235,23 @@ int gls_cell_lut(const gls_cell *cell, const gls_prim *prims, int out,
 
 int gls_abi_version(void);
 
+/* Kahn levels of an instance graph, computed on device `device` (replaces
+ * GenerateAdjacencyList / SetInDegrees / TopologyOrder, src/process.cpp:
+ * 90-176, and the level packing of 423-566).  pred_start[n_inst + 1]
+ * (pred_start[0] = 0, nondecreasing) and pred[] list every instance's
+ * predecessors: the instances driving its input nets (repeats are
+ * harmless).  Level 0 holds the instances without predecessors; every
+ * later level the instances whose predecessors are all placed, in instance
+ * order.  order[n_inst] receives the instances level by level,
+ * level_start[] (room for n_inst + 1 entries) the first position of every
+ * level followed by n_inst, *n_levels the number of levels.  GLS_EINVAL for
+ * a malformed table, a predecessor out of range, or a combinational loop
+ * (the reference degrades a loop to one instance per level,
+ * src/process.cpp:143-155). */
+int gls_levelize(int device, uint32_t n_inst, const uint64_t *pred_start,
+                 const uint32_t *pred, uint32_t *order, uint32_t *level_start,
+                 uint32_t *n_levels);
+
 /* ---------------------------------------------------------------------
  * Learned presize.  No counterpart in the reference, which sizes every
  * gate output from its fan-in rows (src/simulate.cu:2300-2306) and then
