@@ -472,6 +472,47 @@ struct Reader {
             if ((p / W + 1) * W < e) nt = __ldg(P + cb + p / W + 1);
         }
     }
+    // the head after `start`, and after each move
+    __device__ __forceinline__ uint32_t first(const C *__restrict__ P, uint64_t off, uint32_t p0, uint32_t e0)
+    {
+        start(P, off, p0, e0);
+        return head();
+    }
+    __device__ __forceinline__ uint32_t next(const C *__restrict__ P)
+    {
+        advance(P);
+        return head();
+    }
+};
+
+// One-event chunks: the caller keeps the head, the reader only the
+// prefetched event after it, the place of the one after that and the count
+// left (four registers per list).
+template <>
+struct Reader<1> {
+    using C = uint32_t;
+    const uint32_t *q;  // the event after the prefetched one
+    uint32_t left;      // events after the head
+    uint32_t nt;        // the event after the head (when left > 0)
+
+    __device__ __forceinline__ uint32_t first(const C *__restrict__ P, uint64_t off, uint32_t p0, uint32_t e0)
+    {
+        left = 0;
+        if (p0 >= e0) return kInf;
+        const uint32_t *x = P + off + p0;
+        const uint32_t h = __ldg(x);
+        left = e0 - p0 - 1;
+        if (left) nt = __ldg(x + 1);
+        q = x + 2;
+        return h;
+    }
+    __device__ __forceinline__ uint32_t next(const C *__restrict__)
+    {
+        if (!left) return kInf;
+        const uint32_t h = nt;
+        if (--left) nt = __ldg(q++);
+        return h;
+    }
 };
 
 // x * y / z for 32-bit operands, in 32-bit arithmetic when the product fits
@@ -617,8 +658,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
                 before = true;
             }
         }
-        rd[j].start(P, off[j], b, e);
-        hk[j] = rd[j].head();
+        hk[j] = rd[j].first(P, off[j], b, e);
     }
     const uint8_t *lut = a.lut + md.lut_off;
     const NetDelay *nd = a.ndel + md.dt_off;
@@ -641,8 +681,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
             if ((hk[j] | 3u) == mk) {
                 chg |= 1u << j;
                 curp = (curp & ~(3u << (2 * j))) | (ev_val(hk[j]) << (2 * j));
-                rd[j].advance(P);
-                hk[j] = rd[j].head();
+                hk[j] = rd[j].next(P);
             }
         }
         const uint32_t F = kSlut ? slut_get<M>(sl, curp) : lut[lut_index(curp, md)];
