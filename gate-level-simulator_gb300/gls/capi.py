@@ -29,7 +29,7 @@ EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
             "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched",
-            "gls_autotune", "gls_set_schedule", "gls_levelize"]
+            "gls_autotune", "gls_set_schedule", "gls_levelize", "gls_vcd_scan", "gls_vcd_free"]
 
 
 class GlsError(RuntimeError):
@@ -134,6 +134,9 @@ def load_library(path: Path | None = None) -> C.CDLL:
     lib.gls_autotune.argtypes = [C.c_void_p, C.POINTER(BatchOpts), C.POINTER(TuneResult)]
     lib.gls_set_schedule.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]
     lib.gls_levelize.argtypes = [C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.gls_vcd_scan.argtypes = [C.c_int, C.c_char_p, C.c_uint64, C.c_void_p, C.c_void_p]
+    lib.gls_vcd_free.argtypes = [C.c_void_p]
+    lib.gls_vcd_free.restype = None
     lib.gls_set_presize_model.argtypes = [C.c_void_p, C.POINTER(PresizeModel)]
     lib.gls_presize_samples.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -190,6 +193,53 @@ def levelize_gpu(pred_start: np.ndarray, pred: np.ndarray, device: int = 0):
     if rc:
         raise GlsError(rc, "gls_levelize: malformed predecessor table or combinational loop")
     return order[:n], level_start[: nl.value + 1]
+
+
+class VcdIds(C.Structure):
+    _fields_ = [("n_ids", C.c_uint32), ("key", C.c_void_p), ("var_start", C.c_void_p), ("bit_start", C.c_void_p),
+                ("bits", C.c_void_p), ("bus", C.c_void_p)]
+
+
+class VcdChanges(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("signal", C.POINTER(C.c_uint32)), ("time", C.POINTER(C.c_uint64)),
+                ("value", C.POINTER(C.c_uint8)), ("bus", C.POINTER(C.c_uint8)), ("fallback", C.c_int)]
+
+
+def vcd_scan(body: bytes, codes: dict[str, list[tuple[list[int], bool]]], device: int = 0):
+    """Bit changes of a VCD body on the GPU (gls_vcd_scan).  codes: identifier
+    code -> declarations (bit signals msb first, bus flag).  Returns
+    (signal, time, value, bus, fallback) in file order."""
+    lib = load_library()
+    keyed = []
+    for code, decls in codes.items():
+        b = code.encode()
+        if not 0 < len(b) <= 8:
+            raise ValueError("identifier codes of 1 to 8 bytes")
+        keyed.append((int.from_bytes(b, "little"), decls))
+    keyed.sort(key=lambda x: x[0])
+    key = np.array([k for k, _ in keyed], np.uint64)
+    var_start, bit_start, bits, bus = [0], [0], [], []
+    for _, decls in keyed:
+        for sig, is_bus in decls:
+            bits.extend(sig)
+            bit_start.append(len(bits))
+            bus.append(1 if is_bus else 0)
+        var_start.append(len(bus))
+    arrs = [key, np.array(var_start, np.uint32), np.array(bit_start, np.uint32), np.array(bits, np.uint32),
+            np.array(bus, np.uint8)]
+    ids = VcdIds(len(key), *[_ptr(a) if len(a) else None for a in arrs])
+    out = VcdChanges()
+    buf = C.create_string_buffer(body, len(body))
+    rc = lib.gls_vcd_scan(device, buf, len(body), C.byref(ids), C.byref(out))
+    if rc:
+        raise GlsError(rc, "gls_vcd_scan")
+    try:
+        n = int(out.n)
+        take = lambda p, dt: np.ctypeslib.as_array(p, (n,)).astype(dt) if n else np.zeros(0, dt)
+        return (take(out.signal, np.uint32), take(out.time, np.uint64), take(out.value, np.uint8),
+                take(out.bus, np.uint8), bool(out.fallback))
+    finally:
+        lib.gls_vcd_free(C.byref(out))
 
 
 def netlist_preds(in_nets: list[list[int]], out_nets: list[list[int]]):

@@ -1,5 +1,5 @@
 // gls_simulate <inter.dat> <vcd> <dumpon_time> <dumpoff_time> <out.saif>
-//              [--calc fixed|literal] [--device N]
+//              [--calc fixed|literal] [--device N] [--host-vcd]
 //
 // The `simulate` step of the reference (src/simulate.cu:1786-3315) on
 // libgls: read the levelized design and the VCD stimulus, simulate every
@@ -10,6 +10,9 @@
 // nets, gate outputs, constants, assign aliases (with their source's
 // counts) and declared bus bits nothing drives (all X).  Records are written
 // in net order; the reference writes them in hash-map order.
+//
+// The VCD body is scanned on the GPU (gls_vcd_scan) unless --host-vcd is
+// given; both read the same changes.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -29,9 +32,11 @@ int main(int argc, char **argv)
         return 255;
     }
     int calc = GLS_CALC_FIXED, device = 0;
+    bool host_vcd = false;
     for (int k = 6; k < argc; ++k) {
         if (!strcmp(argv[k], "--calc") && k + 1 < argc) calc = !strcmp(argv[++k], "literal") ? GLS_CALC_LITERAL : GLS_CALC_FIXED;
         else if (!strcmp(argv[k], "--device") && k + 1 < argc) device = atoi(argv[++k]);
+        else if (!strcmp(argv[k], "--host-vcd")) host_vcd = true;
     }
     std::ofstream outf(argv[5]);
     if (!outf) {
@@ -51,7 +56,7 @@ int main(int argc, char **argv)
     }
     VcdData vcd;
     const std::string vtext = read_file(argv[2], &err);
-    if (vtext.empty() || !parse_vcd(vtext, vcd, &err)) {
+    if (vtext.empty() || (host_vcd ? !parse_vcd(vtext, vcd, &err) : parse_vcd_gpu(vtext, vcd, &err, device) < 0)) {
         printf("Parse Failed. %s\n", err.c_str());
         return 1;
     }

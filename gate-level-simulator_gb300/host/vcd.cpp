@@ -8,9 +8,11 @@
 // as if it were full width).
 #include "vcd.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cstdlib>
 #include <cstring>
+#include "gls.h"
 
 namespace glsh {
 
@@ -32,12 +34,11 @@ struct Var {
     bool bus;
 };
 
-}  // namespace
-
-bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
-{
+struct Tok {
+    const std::string &s;
     size_t i = 0;
-    auto tok = [&](std::string &t) -> bool {
+    bool next(std::string &t)
+    {
         while (i < s.size() && isspace((unsigned char)s[i])) ++i;
         if (i >= s.size()) return false;
         size_t j = i;
@@ -45,12 +46,19 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
         t.assign(s, i, j - i);
         i = j;
         return true;
-    };
-    auto skip_to_end = [&]() {
+    }
+    void skip_to_end()
+    {
         std::string t;
-        while (tok(t) && t != "$end") {}
-    };
-    std::unordered_map<std::string, std::vector<Var>> vars;   // id -> declarations
+        while (next(t) && t != "$end") {}
+    }
+};
+
+using Vars = std::unordered_map<std::string, std::vector<Var>>;   // code -> declarations
+
+// the header up to and including "$enddefinitions ... $end"
+bool parse_header(Tok &tk, VcdData &v, Vars &vars, std::string *err)
+{
     auto signal = [&](const std::string &name) -> size_t {
         auto it = v.index.find(name);
         if (it != v.index.end()) return it->second;
@@ -62,16 +70,15 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
         return k;
     };
     std::string t;
-    // ---------------------------------------------------------- header
     for (;;) {
-        if (!tok(t)) {
+        if (!tk.next(t)) {
             if (err) *err = "VCD: no $enddefinitions";
             return false;
         }
-        if (t == "$enddefinitions") { skip_to_end(); break; }
+        if (t == "$enddefinitions") { tk.skip_to_end(); return true; }
         if (t == "$timescale") {
             std::string a, all;
-            while (tok(a) && a != "$end") all += a;
+            while (tk.next(a) && a != "$end") all += a;
             size_t k = 0;
             while (k < all.size() && isdigit((unsigned char)all[k])) ++k;
             v.time_res = k ? (unsigned)atoi(all.substr(0, k).c_str()) : 1u;
@@ -81,7 +88,7 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
         if (t == "$var") {
             std::vector<std::string> f;
             std::string a;
-            while (tok(a) && a != "$end") f.push_back(a);
+            while (tk.next(a) && a != "$end") f.push_back(a);
             if (f.size() < 4) {
                 if (err) *err = "VCD: short $var";
                 return false;
@@ -124,12 +131,18 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
             vars[id].push_back(var);
             continue;
         }
-        if (t[0] == '$') skip_to_end();
+        if (t[0] == '$') tk.skip_to_end();
     }
-    // ------------------------------------------------------------ body
-    std::vector<uint8_t> last(v.names.size(), 2);   // bus bits: the last value kept, starting from Z
-    uint64_t now = 0;
-    auto put = [&](size_t k, uint8_t val, bool dedup) {
+}
+
+// appends changes: bus bits keep only real changes, starting from Z, and a
+// later change at the same time replaces an earlier one
+struct Sink {
+    VcdData &v;
+    std::vector<uint8_t> last;   // bus bits: the last value kept
+    explicit Sink(VcdData &d) : v(d), last(d.names.size(), 2) {}
+    void put(size_t k, uint8_t val, bool dedup, uint64_t now)
+    {
         auto &tt = v.times[k];
         auto &vv = v.values[k];
         if (dedup) {
@@ -142,20 +155,27 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
         }
         tt.push_back(now);
         vv.push_back(val);
-    };
-    while (tok(t)) {
+    }
+};
+
+void parse_body(Tok &tk, VcdData &v, const Vars &vars)
+{
+    Sink sink(v);
+    uint64_t now = 0;
+    std::string t;
+    while (tk.next(t)) {
         const char c = t[0];
         if (c == '#') {
             now = strtoull(t.c_str() + 1, nullptr, 10);
             continue;
         }
         if (c == '$') {
-            if (t == "$comment") skip_to_end();
+            if (t == "$comment") tk.skip_to_end();
             continue;   // $dumpvars / $dumpall / $dumpon / $dumpoff / $end
         }
         if (c == 'b' || c == 'B') {
             std::string id;
-            if (!tok(id)) break;
+            if (!tk.next(id)) break;
             auto it = vars.find(id);
             if (it == vars.end()) continue;
             std::string bits = t.substr(1);
@@ -168,14 +188,14 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
                 const size_t off = full.size() - var.bits.size();
                 for (size_t b = 0; b < var.bits.size(); ++b) {
                     const uint8_t val = code(full[off + b]);
-                    if (val != 255) put(var.bits[b], val, var.bus);
+                    if (val != 255) sink.put(var.bits[b], val, var.bus, now);
                 }
             }
             continue;
         }
         if (c == 'r' || c == 'R') {
             std::string id;
-            tok(id);
+            tk.next(id);
             continue;
         }
         const uint8_t val = code(c);
@@ -183,9 +203,73 @@ bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
         auto it = vars.find(t.substr(1));
         if (it == vars.end()) continue;
         for (const Var &var : it->second)
-            for (size_t k : var.bits) put(k, val, var.bus);
+            for (size_t k : var.bits) sink.put(k, val, var.bus, now);
     }
+}
+
+}  // namespace
+
+bool parse_vcd(const std::string &s, VcdData &v, std::string *err)
+{
+    Tok tk{s};
+    Vars vars;
+    if (!parse_header(tk, v, vars, err)) return false;
+    parse_body(tk, v, vars);
     return true;
+}
+
+int parse_vcd_gpu(const std::string &s, VcdData &v, std::string *err, int device)
+{
+    Tok tk{s};
+    Vars vars;
+    if (!parse_header(tk, v, vars, err)) return -1;
+    // the code table: keys of at most 8 bytes, sorted
+    std::vector<std::pair<uint64_t, const std::vector<Var> *>> codes;
+    bool fits = true;
+    for (const auto &kv : vars) {
+        const std::string &id = kv.first;
+        if (id.empty() || id.size() > 8) { fits = false; break; }
+        uint64_t key = 0;
+        for (size_t j = 0; j < id.size(); ++j) key |= (uint64_t)(uint8_t)id[j] << (8 * j);
+        codes.emplace_back(key, &kv.second);
+    }
+    const size_t body = tk.i, n = s.size() - body;
+    if (!fits || n >= 0xFFFFFFFFull) {
+        parse_body(tk, v, vars);
+        return 0;
+    }
+    std::sort(codes.begin(), codes.end(),
+              [](const std::pair<uint64_t, const std::vector<Var> *> &a,
+                 const std::pair<uint64_t, const std::vector<Var> *> &b) { return a.first < b.first; });
+    std::vector<uint64_t> key;
+    std::vector<uint32_t> var_start(1, 0), bit_start(1, 0), bits;
+    std::vector<uint8_t> bus;
+    for (const auto &c : codes) {
+        key.push_back(c.first);
+        for (const Var &var : *c.second) {
+            for (size_t b : var.bits) bits.push_back((uint32_t)b);
+            bit_start.push_back((uint32_t)bits.size());
+            bus.push_back(var.bus ? 1 : 0);
+        }
+        var_start.push_back((uint32_t)bus.size());
+    }
+    gls_vcd_ids ids{(uint32_t)key.size(), key.data(), var_start.data(), bit_start.data(), bits.data(), bus.data()};
+    gls_vcd_changes ch;
+    const int rc = gls_vcd_scan(device, s.data() + body, n, &ids, &ch);
+    if (rc || ch.fallback) {
+        gls_vcd_free(&ch);
+        if (rc && rc != GLS_ERANGE) {
+            if (err) *err = "VCD: GPU scan failed (code " + std::to_string(rc) + ")";
+            return -1;
+        }
+        parse_body(tk, v, vars);
+        return 0;
+    }
+    Sink sink(v);
+    for (uint64_t r = 0; r < ch.n; ++r)
+        if (ch.value[r] != 255) sink.put(ch.signal[r], ch.value[r], ch.bus[r] != 0, ch.time[r]);
+    gls_vcd_free(&ch);
+    return 1;
 }
 
 }  // namespace glsh

@@ -252,6 +252,42 @@ int gls_levelize(int device, uint32_t n_inst, const uint64_t *pred_start,
                  const uint32_t *pred, uint32_t *order, uint32_t *level_start,
                  uint32_t *n_levels);
 
+/* VCD body scan on the GPU (replaces VCDParser::parse_core / combine_core /
+ * core, src/VCDParser.cpp:508-644, 458-507, 194-242, for the text after
+ * $enddefinitions; the header stays with the caller).  The identifier codes
+ * of the header's $var lines, at most 8 bytes each, as little-endian keys
+ * (zero-padded), strictly increasing; var_start[n_ids + 1] their
+ * declarations; bit_start[n_vars + 1] each declaration's bits (msb first),
+ * bits[] the signal of every bit, bus[n_vars] 1 for a bus declaration. */
+typedef struct gls_vcd_ids {
+    uint32_t n_ids;
+    const uint64_t *key;
+    const uint32_t *var_start;
+    const uint32_t *bit_start;
+    const uint32_t *bits;
+    const uint8_t *bus;
+} gls_vcd_ids;
+/* Every bit change in file order: signal, time in force, value (0, 1=X,
+ * 2=Z, 3; 255 for a character that is no value, which the reference
+ * skips) and whether the bit belongs to a bus declaration (the caller keeps
+ * only real changes of those, starting from Z, and lets a later change at
+ * the same time replace an earlier one, as the reference does).
+ * fallback = 1: the body reads differently token by token (an identifier
+ * code equal to $comment or $end); parse it on the host instead. */
+typedef struct gls_vcd_changes {
+    uint64_t n;
+    uint32_t *signal;
+    uint64_t *time;
+    uint8_t *value;
+    uint8_t *bus;
+    int fallback;
+} gls_vcd_changes;
+/* Scan n_bytes (< 2^32) of body text on device `device`; the arrays of
+ * *out are allocated by the library, released by gls_vcd_free. */
+int gls_vcd_scan(int device, const char *body, uint64_t n_bytes, const gls_vcd_ids *ids,
+                 gls_vcd_changes *out);
+void gls_vcd_free(gls_vcd_changes *out);
+
 /* ---------------------------------------------------------------------
  * Learned presize.  No counterpart in the reference, which sizes every
  * gate output from its fan-in rows (src/simulate.cu:2300-2306) and then
