@@ -13,9 +13,11 @@
 //                        that later segments make into earlier ones, settles
 //                        the one undecided duplicate at each segment bottom
 //                        and places the segments in the gate's pool slot.
-//   k_copy     (1 warp per segment) moves the kept entries from the level
+//   k_copy     (8 lanes per segment) moves the kept entries from the level
 //                        scratch into the event pool and accumulates T0/T1/TX
 //                        (fused SAIF).
+//   k_sim_warp<M> (optional per fan-in class: a warp per segment) is the
+//                        same contract as k_sim, merged by tiles.
 //
 // Semantics follow src/simulate.cpp:872-1506 of the reference.  Why the
 // segment split is exact: a candidate output event k (time o_k) is removed
@@ -770,7 +772,10 @@ template <int M, bool kBatch>
 #ifndef GLS_SIM3_BLOCKS
 #define GLS_SIM3_BLOCKS 8   // resident blocks per SM the 3-input gate kernel is compiled for
 #endif
-__global__ void __launch_bounds__(128, M <= 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4))
+#ifndef GLS_SIM1_BLOCKS
+#define GLS_SIM1_BLOCKS GLS_SIM2_BLOCKS   // resident blocks per SM the 1-input gate kernel is compiled for
+#endif
+__global__ void __launch_bounds__(128, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4)))
     k_sim(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     __shared__ uint32_t s_next;
@@ -1332,7 +1337,10 @@ __device__ __forceinline__ void saif_add(unsigned long long acc[3], int cls, uns
 // before it, places the segments back to back in the gate's pool slot and
 // hands each segment's copy to k_copy with the final event that precedes it.
 template <bool kBatch>
-__global__ void __launch_bounds__(256) k_link(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
+#ifndef GLS_LINK_BLOCKS
+#define GLS_LINK_BLOCKS 1   // resident blocks per SM the link kernel is compiled for (1: no bound)
+#endif
+__global__ void __launch_bounds__(256, GLS_LINK_BLOCKS) k_link(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     // gate outputs [d0, d1) of the level (one fan-in class, or all)
     const uint32_t n = d1 - d0;
@@ -1688,7 +1696,7 @@ static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, 
         default: break;
         }
     }
-    const int grid = sm_count * (cls <= 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4));
+    const int grid = sm_count * (cls == 0 ? GLS_SIM1_BLOCKS : (cls == 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4)));
     switch (cls) {
     case 0: k_sim<1, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
     case 1: k_sim<2, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
