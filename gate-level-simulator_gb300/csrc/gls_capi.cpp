@@ -657,8 +657,14 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         }
     };
     const unsigned hc = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    if (total > (1u << 20) && hc > 1 && st->n_nets > 4 * hc) {
-        if (!ctx->pool) ctx->pool = new WorkPool(hc - 1);
+    if (total > (1u << 20) && hc > 1 && st->n_nets > 4 * hc && !ctx->pool) {
+        try {
+            ctx->pool = new WorkPool(hc - 1);
+        } catch (...) {   // no threads to be had: pack on this one
+            ctx->pool = nullptr;
+        }
+    }
+    if (total > (1u << 20) && ctx->pool && st->n_nets > 4 * ctx->pool->threads()) {
         // parts of about equal event counts: part q starts at the first net
         // whose packed offset reaches q * total / parts
         const unsigned parts = 4 * ctx->pool->threads();

@@ -20,17 +20,14 @@ class WorkPool {
 public:
     explicit WorkPool(unsigned threads)
     {
-        for (unsigned i = 0; i < threads; ++i) th_.emplace_back([this] { loop(); });
-    }
-    ~WorkPool()
-    {
-        {
-            std::lock_guard<std::mutex> l(mu_);
-            stop_ = true;
+        try {
+            for (unsigned i = 0; i < threads; ++i) th_.emplace_back([this] { loop(); });
+        } catch (...) {   // the threads started so far end before the error leaves
+            shutdown();
+            throw;
         }
-        cv_.notify_all();
-        for (auto &t : th_) t.join();
     }
+    ~WorkPool() { shutdown(); }
     unsigned threads() const { return (unsigned)th_.size() + 1; }
     void parallel_for(unsigned n, const std::function<void(unsigned)> &f)
     {
@@ -50,6 +47,17 @@ public:
     }
 
 private:
+    void shutdown()
+    {
+        {
+            std::lock_guard<std::mutex> l(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_)
+            if (t.joinable()) t.join();
+        th_.clear();
+    }
     void work()
     {
         for (;;) {

@@ -23,8 +23,8 @@ struct VcdData {
 bool parse_vcd(const std::string &text, VcdData &v, std::string *err);
 // The same with the body scanned on GPU `device` (gls_vcd_scan): 1 when the
 // GPU read the body, 0 when the host did (codes longer than 8 bytes, a body
-// of 4 GB or more, or a body the token-parallel scan reads differently),
-// -1 on an error.
+// of 4 GB or more, a body the token-parallel scan reads differently, or a
+// failed scan), -1 on an error in the header.
 int parse_vcd_gpu(const std::string &text, VcdData &v, std::string *err, int device);
 
 }  // namespace glsh
