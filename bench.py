@@ -220,10 +220,9 @@ def reference_arm(args):
 def gls_arm(args):
     import torch
     from gls.capi import Simulator
+    from gls.replicas import max_over_ranks, rank_seed, whole_job_rate, world_rank
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = world_rank()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -231,7 +230,7 @@ def gls_arm(args):
     stream = torch.cuda.current_stream()
     cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
     # replicas: every rank simulates its own independent window (weak scaling)
-    st = stimulus_for(cfg, nl, args.seed + 1 + 1000 * rank)
+    st = stimulus_for(cfg, nl, rank_seed(args.seed, rank))
     from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED
     alloc = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}[args.alloc]
     sim = Simulator(device=local, stream=stream.cuda_stream, seg_events=args.seg, alloc_mode=alloc)
@@ -283,13 +282,10 @@ def gls_arm(args):
                      "overflow_rate": stats["presize_overflows"] / max(1, len(c)), "margin": margin,
                      "mae_events": q["mae_events"], "mae_log": q["mae_log"],
                      "reserve_over_exact": q["reserve_over_exact"]}
-    if world > 1:
-        t = torch.tensor([step_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(step_ms, "cuda")
     gate_ev = stats["gate_events"]
-    value = gate_ev * world / (step_ms / 1000.0)
-    sim_cycles = cfg.cycles * world / (step_ms / 1000.0)
+    value = whole_job_rate(gate_ev, world, step_ms / 1000.0)
+    sim_cycles = whole_job_rate(cfg.cycles, world, step_ms / 1000.0)
     # end to end through the C ABI with host buffers
     pinned = {k: torch.from_numpy(np.ascontiguousarray(getattr(st, k))).pin_memory().numpy()
               for k in ("nets", "ev_start", "time", "value")}
@@ -313,11 +309,8 @@ def gls_arm(args):
         sim.clear_windows()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = gate_ev * world / e2e_s
+    e2e_s = max_over_ranks(e2e_s, "cuda")
+    e2e = whole_job_rate(gate_ev, world, e2e_s)
     # roofline of the dominant kernel (k_sim): algorithmic bytes per step =
     # fan-in events read (5 B each per distinct net) + output events written
     # (5 B) + gate metadata (48 B) and arcs (16 B); divided by its event time.
