@@ -411,7 +411,7 @@ extern "C" int gls_vcd_scan(int device, const char *body, uint64_t n_bytes, cons
 {
     if (!out || !ids || (n_bytes && !body)) return GLS_EINVAL;
     std::memset(out, 0, sizeof *out);
-    if (n_bytes >= 0xFFFFFFFFull) return GLS_ERANGE;   // positions are 32-bit
+    if (n_bytes >= 0xFFFF0000ull) return GLS_ERANGE;   // positions (and a tile's end) stay 32-bit
     if (n_bytes == 0) return GLS_OK;
     const uint32_t n = (uint32_t)n_bytes;
     const uint32_t n_vars = ids->var_start[ids->n_ids];

@@ -234,7 +234,7 @@ int parse_vcd_gpu(const std::string &s, VcdData &v, std::string *err, int device
         codes.emplace_back(key, &kv.second);
     }
     const size_t body = tk.i, n = s.size() - body;
-    if (!fits || n >= 0xFFFFFFFFull) {
+    if (!fits || n >= 0xFFFF0000ull) {
         parse_body(tk, v, vars);
         return 0;
     }

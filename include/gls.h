@@ -282,7 +282,7 @@ typedef struct gls_vcd_changes {
     uint8_t *bus;
     int fallback;
 } gls_vcd_changes;
-/* Scan n_bytes (< 2^32) of body text on device `device`; the arrays of
+/* Scan n_bytes (< 2^32 - 2^16) of body text on device `device`; the arrays of
  * *out are allocated by the library, released by gls_vcd_free. */
 int gls_vcd_scan(int device, const char *body, uint64_t n_bytes, const gls_vcd_ids *ids,
                  gls_vcd_changes *out);
