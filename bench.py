@@ -1,20 +1,30 @@
 #!/usr/bin/env python
 """Benchmark of the simulate stage on one GB300 (or N replicas).
 
-Workload (default `c2`, the medium configuration): a synthetic levelized
-netlist of 200,000 GEN_*_D1 cells, depth 60, 4,096 pseudo-primary inputs, a
-10,000-cycle clocked stimulus (1,000 ps period, Beta(2,8) toggle rates),
-window 0..10,000,000 ps.  One step = one pass of the hot path over one
-stimulus window: every level simulated on the GPU plus the fused SAIF counts.
+Workload (default `c3`, the large configuration): a synthetic levelized
+netlist of 2,000,000 GEN_*_D1 cells, depth 120, 65,536 pseudo-primary
+inputs, a 20,000-cycle clocked stimulus (1,000 ps period, toggle rates
+log-uniform in [0.01, 0.5]), window 0..20,000,000 ps, simulated with the
+learned presize (`--alloc learned`).  One step = one pass of the hot path
+over one stimulus window: every level simulated on the GPU plus the fused
+SAIF counts.
 
-  value   gate-events/s with the stimulus resident in HBM (device time from
-          CUDA events on the launch stream)
-  e2e     the same metric through the C ABI with host buffers: stimulus
-          upload from pinned memory, run, SAIF counts back to the host
-  --impl reference   the reference's own serial simulator core
-          (oracle/_ref, built from the reference sources) on this host's
-          cores, on a fixed-seed sample of gates fed their exact input
-          waveforms (computed beforehand by the CPU oracle).
+  value        gate-events/s with the stimulus resident in HBM (device time
+               from CUDA events on the launch stream)
+  e2e          the same metric through the C ABI with host buffers: stimulus
+               upload from pinned memory, run, SAIF counts back to the host
+  plain_exact  the same workload with the plain exact count-then-fill
+               allocation, device-timed the same way, and value / plain
+  parity       a fixed-seed sample of gates from every level, each fed its
+               input waveforms as the GPU produced them, run through the
+               reference's own serial core (oracle/_ref, built from the
+               reference sources); its output waveforms and SAIF counts are
+               compared with the GPU's bit for bit
+  cpu_baseline the same reference run, timed on this host's cores
+  --impl reference   the reference's own serial simulator core on this
+               host's cores, on a fixed-seed sample of gates fed their exact
+               input waveforms (computed beforehand by the CPU oracle, which
+               keeps only the lists still to be read)
 """
 from __future__ import annotations
 
@@ -48,6 +58,18 @@ def workload_desc(args) -> str:
         return (f"{args.config} generator scaled: cells={args.cells or 'default'}, depth={args.depth or 'default'}, "
                 f"cycles={args.cycles or 'default'} (profiling case, not the benchmark workload)")
     return base
+
+
+def bench_config(args) -> dict:
+    """The `config` object; both arms print the same one."""
+    cfg = {"workload": workload_desc(args), "seed": args.seed, "alloc": args.alloc,
+           "parallelism": f"replicas x{args.gpus}"}
+    if args.config == "c4":
+        cfg["windows"] = args.windows or C4_WINDOWS
+        cfg["l2"] = "every step streams GBs of event pool per window (> L2)"
+    else:
+        cfg["l2"] = "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)"
+    return cfg
 
 
 def log(*a):
@@ -126,100 +148,105 @@ def stimulus_for(cfg, nl, seed):
     return st
 
 
-# ------------------------------------------------------------- reference leg
-def sample_case(nl, waves_of, k, seed):
-    """k gates drawn with a fixed seed from all levels, rewired as independent
-    single gates whose inputs are stimulus nets carrying their exact input
-    waveforms.  Returns (netlist, stimulus, gate_events)."""
-    from gls.levelize import assemble
-    from gls.netlist import Stimulus
-    rng = np.random.default_rng(seed)
-    pick = np.sort(rng.choice(nl.n_inst, size=min(k, nl.n_inst), replace=False))
-    insts, stim, nxt, gev = [], {}, 0, 0
-    for i in pick:
-        c = nl.cells[int(nl.inst_cell[i])]
-        src = nl.inputs_of(int(i))
-        local = {}
-        ins = []
-        for n in src.tolist():
-            if n not in local:
-                local[n] = nxt
-                stim[nxt] = waves_of(n)
-                nxt += 1
-            ins.append(local[n])
-            gev += len(stim[local[n]][0])
-        arcs = [(int(a["edge"]), int(a["in_pin"]), int(a["out_pin"]), float(a["rise"]), float(a["fall"]))
-                for a in nl.arcs[int(nl.arc_start[i]): int(nl.arc_start[i + 1])]]
-        insts.append((c.name, ins, [-1] * c.n_out, arcs))
-    for inst in insts:
-        inst[2][:] = list(range(nxt, nxt + len(inst[2])))
-        nxt += len(inst[2])
-    sn = sorted(stim)
-    ev = np.zeros(len(sn) + 1, np.uint64)
-    ev[1:] = np.cumsum([len(stim[n][0]) for n in sn])
-    T = np.concatenate([np.asarray(stim[n][0], np.uint32) for n in sn]) if sn else np.zeros(0, np.uint32)
-    V = np.concatenate([np.asarray(stim[n][1], np.uint8) for n in sn]) if sn else np.zeros(0, np.uint8)
-    return assemble(insts, n_nets=nxt), Stimulus(np.array(sn, np.uint32), ev, T, V), gev
+def sample_desc(r, what):
+    from oracle.sample import SAMPLE_SEED
+    return (f"{r['gates']} gates sampled (seed {SAMPLE_SEED}) from all levels, each fed {what}; "
+            f"{r['gev']} gate-events in {r['sec']:.2f}s")
 
 
-def time_reference_sample(nl, waves_of, t_end, threads, budget_s=8.0, seed=7, max_k=4000):
-    """Time the reference core on a sample sized to ~budget_s of wall time.
-    -> (gate-events/s, description, kind, threads)."""
-    from oracle import build as obuild
-    from oracle.runner import run_oracle, run_reference
-    have_ref = obuild.build_reference() is not None
-    k = 24
-    while True:
-        snl, sst, gev = sample_case(nl, waves_of, k, seed)
-        if have_ref:
-            _, _, sec = run_reference(snl, sst, 0, t_end, threads=threads)
-        else:
-            _, _, sec = run_oracle(snl, sst, 0, t_end, threads=threads)
-        if sec >= budget_s / 3 or k >= max_k or k >= nl.n_inst:
-            break
-        k = min(max_k, nl.n_inst, int(k * max(2.0, budget_s / max(sec, 1e-3) * 0.8)))
-    kind = "reference" if have_ref else "port"
-    desc = (f"{len(snl.inst_cell)} gates sampled (seed {seed}) from all levels, each fed its exact "
-            f"input waveforms; {gev} gate-events in {sec:.2f}s")
-    return gev / sec, desc, kind, sec, snl, sst, gev
-
-
+# ------------------------------------------------------------- reference arm
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from gls.replicas import rank_seed
     from oracle.runner import run_oracle
+    from oracle.sample import sample_input_nets, sample_order, sized_sample
     cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
-    st = stimulus_for(cfg, nl, args.seed + 1)
+    st = stimulus_for(cfg, nl, rank_seed(args.seed, 0))
     threads = os.cpu_count() or 1
+    order = sample_order(nl)
+    keep = sample_input_nets(nl, order)
     t0 = time.time()
-    ow, _, _ = run_oracle(nl, st, 0, cfg.t_end, threads=threads)
-    log(f"oracle port produced the exact waveforms in {time.time() - t0:.1f}s")
-    rate, desc, kind, sec, snl, sst, gev = time_reference_sample(nl, lambda n: ow[n], cfg.t_end, threads)
-    from oracle.runner import run_oracle as ro, run_reference as rr
+    # exact input waveforms of the sample: the C oracle over the whole
+    # design, keeping only the sampled gates' input lists (every other list
+    # is dropped after the last level that reads it)
+    ow, _, _ = run_oracle(nl, st, 0, cfg.t_end, threads=threads, keep=keep)
+    log(f"oracle port produced the sample's exact input waveforms in {time.time() - t0:.1f}s")
+    r = sized_sample(nl, lambda n: ow[n], cfg.t_end, threads, order, args.ref_budget)
+    snl, sst, run = r["snl"], r["sst"], r["run"]
     for _ in range(args.warmup):
-        (rr if kind == "reference" else ro)(snl, sst, 0, cfg.t_end, threads=threads)
+        run(snl, sst, 0, cfg.t_end, threads=threads)
     times = []
     for _ in range(args.steps):
-        _, _, s = (rr if kind == "reference" else ro)(snl, sst, 0, cfg.t_end, threads=threads)
+        _, _, s = run(snl, sst, 0, cfg.t_end, threads=threads)
         times.append(s)
-    v = gev / float(np.mean(times))
+    v = r["gev"] / float(np.mean(times))
+    one = single_core(nl, lambda n: ow[n], cfg.t_end, order, r)
     line = {
         "impl": "reference", "metric": "gate-events/s", "value": v, "unit": "gate-events/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * float(np.mean(times)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": workload_desc(args), "seed": args.seed},
-        "cpu_baseline": {"value": v, "unit": "gate-events/s", "cores": threads, "kind": kind, "sample": desc},
+        "config": bench_config(args),
+        "cpu_baseline": {"value": v, "unit": "gate-events/s", "cores": threads, "kind": r["kind"],
+                         "sample": sample_desc(r, "its exact input waveforms (C oracle over the whole design)"),
+                         "single_core": one},
         "e2e": {"value": v, "unit": "gate-events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def single_core(nl, waves_of, t_end, order, r, budget_s=4.0):
+    """The reference core on one thread (the reference's own loop is
+    serial), on a prefix of the sample sized to about budget_s."""
+    from oracle.sample import run_sample
+    threads = os.cpu_count() or 1
+    k = max(1, min(r["gates"], int(r["gates"] * budget_s / max(r["sec"] * threads, 1e-3))))
+    one = run_sample(nl, waves_of, order[:k], 0, t_end, 1)
+    return {"value": one["rate"], "unit": "gate-events/s", "cores": 1,
+            "sample": f"the first {k} gates of the sample; {one['gev']} gate-events in {one['sec']:.2f}s"}
+
+
 # ------------------------------------------------------------------ GPU arm
+def device_timed_runs(sim, stream, flush, steps):
+    """Mean device ms of `steps` runs (CUDA events on the launch stream, L2
+    flushed before every run)."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        sim.run()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in ev]))
+
+
+def make_sim(args, alloc, local, stream, **kw):
+    from gls.capi import Simulator
+    sim = Simulator(device=local, stream=stream.cuda_stream, seg_events=args.seg, alloc_mode=alloc, **kw)
+    if args.alloc == "learned":
+        from gls import presize
+        sim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
+    return sim
+
+
+def parity_check(sim, r, w=0):
+    """The sampled gates' outputs as the GPU made them against the reference
+    core's, bit for bit (waveforms and SAIF counts)."""
+    from oracle.sample import compare_outputs
+    out = compare_outputs(lambda n: sim.waveform(int(n), w), sim.saif(w), r)
+    out["how"] = ("each sampled gate fed its input waveforms as the GPU produced them, run through "
+                  + ("the reference's own serial core (oracle/_ref)" if r["kind"] == "reference"
+                     else "the C oracle") + "; output waveform and T0/T1/TX compared bit for bit")
+    return out
+
+
 def gls_arm(args):
     import torch
-    from gls.capi import Simulator
+    from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED
     from gls.replicas import max_over_ranks, rank_seed, whole_job_rate, world_rank
 
     world, rank, local = world_rank()
@@ -231,12 +258,9 @@ def gls_arm(args):
     cfg, nl = make_workload(args.config, args.seed, args.cells, args.depth, args.cycles)
     # replicas: every rank simulates its own independent window (weak scaling)
     st = stimulus_for(cfg, nl, rank_seed(args.seed, rank))
-    from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED
-    alloc = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}[args.alloc]
-    sim = Simulator(device=local, stream=stream.cuda_stream, seg_events=args.seg, alloc_mode=alloc)
-    if args.alloc == "learned":
-        from gls import presize
-        sim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
+    modes = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}
+    alloc = modes[args.alloc]
+    sim = make_sim(args, alloc, local, stream)
     sim.load(nl)
     w = sim.add_window(st, 0, cfg.t_end)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
@@ -251,25 +275,17 @@ def gls_arm(args):
         tune = {"best": {"seg_per_sm": seg_sm, "warp_mask": mask, "flags": flags}, "candidates": []}
     else:
         tune = sim.autotune()   # untimed: the schedule for this workload (results never depend on it)
+    sched = {k: tune["best"][k] for k in ("seg_per_sm", "warp_mask", "flags")}
     log(f"autotune: {tune['best']}; candidates (segments/SM, warp mask, flags: ms): " +
         ", ".join(f"{c['seg_per_sm']}/{c['warp_mask']}/{c['flags']}: {c['ms']:.2f}" for c in tune["candidates"]))
     for _ in range(args.warmup):
         sim.run()
     stats = sim.stats()
     # device-timed region: stimulus resident in HBM
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    sim_ms = comb_ms = plan_ms = 0.0
     barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for k in range(args.steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            sim.run()
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+        step_ms = device_timed_runs(sim, stream, flush, args.steps)
     barrier()
-    step_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
 
     presize_q = None
     if args.alloc == "learned":
@@ -305,21 +321,18 @@ def gls_arm(args):
     for _ in range(args.steps):
         wid = sim.add_window(pst, 0, cfg.t_end)
         sim.run()
-        counts = sim.saif(wid)
+        sim.saif(wid)
         sim.clear_windows()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(e2e_s, "cuda")
     e2e = whole_job_rate(gate_ev, world, e2e_s)
-    # roofline of the dominant kernel (k_sim): algorithmic bytes per step =
-    # fan-in events read (5 B each per distinct net) + output events written
-    # (5 B) + gate metadata (48 B) and arcs (16 B); divided by its event time.
+    cpu = parity = None
     if rank == 0 and not args.no_cpu_baseline:
-        # the reference core on a sample, fed exact waveforms from this run
-        sim.clear_windows()
+        # the reference core on a sample of gates fed the GPU's own input
+        # waveforms: a bit-exact check of those gates, and the CPU timing
         sim.add_window(st, 0, cfg.t_end)
         sim.run()
-        threads = os.cpu_count() or 1
         cache = {}
 
         def waves_of(n):
@@ -327,61 +340,75 @@ def gls_arm(args):
                 cache[n] = sim.waveform(int(n), 0)
             return cache[n]
 
-        cpu = time_reference_sample(nl, waves_of, cfg.t_end, threads)
+        from oracle.sample import sample_order, sized_sample
+        t0 = time.time()
+        cpu = sized_sample(nl, waves_of, cfg.t_end, os.cpu_count() or 1, sample_order(nl), 8.0)
+        parity = parity_check(sim, cpu)
+        log(f"parity sample: {parity['gates_checked']} gates, {parity['mismatches']} mismatches "
+            f"({time.time() - t0:.1f}s)")
     sim.close()
+    # the plain exact count-then-fill form on the same workload and schedule
+    plain = None
+    if args.alloc != "exact" and not args.no_plain:
+        psim = make_sim(args, ALLOC_EXACT, local, stream)
+        psim.load(nl)
+        psim.set_schedule(sched["seg_per_sm"], sched["warp_mask"], sched["flags"])
+        psim.add_window(st, 0, cfg.t_end)
+        for _ in range(max(2, args.warmup // 2)):
+            psim.run()
+        barrier()
+        plain_ms = max_over_ranks(device_timed_runs(psim, stream, flush, args.steps), "cuda")
+        pstats = psim.stats()
+        psim.close()
+        plain = {"value": whole_job_rate(pstats["gate_events"], world, plain_ms / 1000.0), "unit": "gate-events/s",
+                 "ms_per_step": plain_ms, "pool_used_bytes": 4 * pstats["pool_used"],
+                 "what": "the same window with exact count-then-fill allocation, same schedule, device-timed",
+                 "value_over_plain": plain_ms / step_ms}
     # kernel-class times (for the roofline) from a profiled twin, made after
     # the timed context is gone: it brackets the classes with events, so they
     # run one after another there
-    psim = Simulator(device=local, stream=stream.cuda_stream, profile=True, seg_events=args.seg, alloc_mode=alloc)
-    if args.alloc == "learned":
-        from gls import presize
-        psim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
-    psim.load(nl)
-    psim.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"], tune["best"]["flags"])
-    psim.add_window(st, 0, cfg.t_end)
-    psim.run()
-    for _ in range(args.steps):
+    prof_steps = min(args.steps, 5)
+    tsim = make_sim(args, alloc, local, stream, profile=True)
+    tsim.load(nl)
+    tsim.set_schedule(sched["seg_per_sm"], sched["warp_mask"], sched["flags"])
+    tsim.add_window(st, 0, cfg.t_end)
+    tsim.run()
+    sim_ms = comb_ms = plan_ms = 0.0
+    for _ in range(prof_steps):
         flush.zero_()
-        psim.run()
-        s = psim.stats()
+        tsim.run()
+        s = tsim.stats()
         sim_ms += s["sim_ms"]
         comb_ms += s["combine_ms"]
         plan_ms += s["plan_ms"]
-    psim.close()
+    tsim.close()
     n_drv = int(nl.n_inst)
+    # algorithmic bytes of the gate kernels per step: fan-in events read
+    # (5 B each per distinct input net), output events written (5 B), gate
+    # metadata (48 B) and arcs (16 B)
     sim_bytes = stats["fanin_bytes"] + 5 * stats["output_events"] + 48 * n_drv + 16 * int(len(nl.arcs))
-    sim_ms_step = sim_ms / args.steps
+    sim_ms_step = sim_ms / prof_steps
     achieved = sim_bytes / (sim_ms_step / 1000.0) / 1e9
     peak, src = peak_hbm()
-    # DRAM bytes of the k_sim launches of one step, from an ncu capture of
-    # this workload (one-pass metrics; profiles/k_sim_c2-depth6-profiling-case.md)
-    traffic = None
-    tp = REPO / "profiles" / "k_sim_traffic.json"
-    if tp.exists() and not (args.cells or args.depth or args.cycles):
-        tr = json.loads(tp.read_text())
-        if tr.get("workload") == args.config:
-            traffic = tr.get("bytes_per_step")
+    traffic, traffic_basis = scaled_traffic(args, stats)
     # whole-step algorithmic bytes (fan-in read + outputs written + SAIF)
     step_bytes = sim_bytes + 5 * stats["output_events"] * 2 + 24 * nl.n_nets
     line = {
         "metric": "gate-events/s", "value": value, "unit": "gate-events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": workload_desc(args), "seed": args.seed, "parallelism": f"replicas x{world}",
-                   "l2": "256 MiB buffer written between timed steps; per-step pool is GBs (> L2)",
-                   "seg_events": args.seg or "auto", "alloc": args.alloc,
-                   "schedule": {k: tune["best"][k] for k in ("seg_per_sm", "warp_mask", "flags")}},
+        "config": bench_config(args),
+        "schedule": dict(sched, seg_events=args.seg or "auto"),
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "traffic_basis": "DRAM bytes per step over the k_sim launches, ncu capture of this workload"
-                                      if traffic else None,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_basis": traffic_basis,
                      "peak_source": src,
                      "algorithmic_bytes_per_step": sim_bytes,
-                     "kernel_ms_per_step": {"k_sim": sim_ms_step, "k_combine": comb_ms / args.steps,
-                                            "k_plan": plan_ms / args.steps,
-                                            "timed": "profiled run with the fan-in classes in turn"},
+                     "kernel_ms_per_step": {"k_sim": sim_ms_step, "k_combine": comb_ms / prof_steps,
+                                            "k_plan": plan_ms / prof_steps,
+                                            "timed": f"profiled run with the fan-in classes in turn, "
+                                                     f"mean of {prof_steps}"},
                      "step_achieved_gbs": step_bytes / (step_ms / 1000.0) / 1e9},
         "e2e": {"value": e2e, "unit": "gate-events/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000.0 * e2e_s},
@@ -390,16 +417,36 @@ def gls_arm(args):
         "pool_bytes": stats["pool_bytes"],
         "pool_used_bytes": 4 * stats["pool_used"],
     }
+    if plain is not None:
+        line["plain_exact"] = plain
     if presize_q is not None:
         line["presize"] = presize_q
-    if rank == 0 and not args.no_cpu_baseline:
-        rate, desc, kind, sec, *_ = cpu
-        line["cpu_baseline"] = {"value": rate, "unit": "gate-events/s", "cores": os.cpu_count() or 1,
-                                "kind": kind, "sample": desc}
+    if parity is not None:
+        line["parity"] = parity
+    if cpu is not None:
+        line["cpu_baseline"] = {"value": cpu["rate"], "unit": "gate-events/s", "cores": os.cpu_count() or 1,
+                                "kind": cpu["kind"],
+                                "sample": sample_desc(cpu, "its input waveforms as the GPU produced them")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def scaled_traffic(args, stats):
+    """DRAM bytes of the gate kernels per step, scaled from an ncu capture
+    of a smaller case of the same generator by the fan-in events processed
+    (the kernels' traffic grows with the events they read and write)."""
+    tp = REPO / "profiles" / "k_sim_traffic.json"
+    if not tp.exists() or args.cells or args.depth or args.cycles:
+        return None, None
+    tr = json.loads(tp.read_text())
+    per_ev = tr.get("dram_bytes_per_fanin_event")
+    if not per_ev:
+        return None, None
+    fanin_events = stats["fanin_bytes"] / 5
+    return per_ev * fanin_events, (f"{per_ev:.3f} DRAM bytes per fan-in event over the k_sim launches of "
+                                   f"{tr.get('case', 'a smaller case')} (ncu), times this step's fan-in events")
 
 
 def batched_arm(args):
@@ -482,11 +529,11 @@ def batched_arm(args):
         "metric": "gate-events/s", "value": gate_ev / dev_s, "unit": "gate-events/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": workload_desc(args), "seed": args.seed, "windows": n_win,
-                   "cycles": int(lengths.sum()), "alloc": args.alloc, "parallelism": "replicas x1",
-                   "l2": "every step streams GBs of event pool per window (> L2)",
-                   "schedule": tune["best"], "value_timing": "device time of the waves (stimulus uploads "
-                   "between waves excluded); e2e: wall clock of add_window + run_batched + SAIF reads"},
+        "config": bench_config(args),
+        "schedule": tune["best"],
+        "cycles": int(lengths.sum()),
+        "value_timing": "device time of the waves (stimulus uploads between waves excluded); e2e: wall clock "
+                        "of add_window + run_batched + SAIF reads",
         "sim_cycles_per_s": float(lengths.sum()) / dev_s,
         "gate_events_per_step": gate_ev,
         "e2e": {"value": gate_ev / step_s, "unit": "gate-events/s",
@@ -508,11 +555,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gls", choices=["gls", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--config", default="c3", choices=sorted(WORKLOADS))
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--seg", type=int, default=0, help="fan-in events per time segment (0 = library default)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--alloc", default="bound", choices=["bound", "exact", "learned"],
+    ap.add_argument("--no-cpu-baseline", action="store_true",
+                    help="skip the reference sample (parity check and CPU timing)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain exact-allocation comparison")
+    ap.add_argument("--alloc", default="learned", choices=["bound", "exact", "learned"],
                     help="gate-output slot allocation: upper bound, exact, or learned presize")
     ap.add_argument("--model", default=None, help="presize model (.npz) for --alloc learned")
     ap.add_argument("--cells", type=int, default=None, help="override the cell count (profiling cases)")
@@ -521,6 +570,8 @@ def main():
     ap.add_argument("--windows", type=int, default=None, help="c4: number of windows (default 256)")
     ap.add_argument("--schedule", default=None,
                     help="c1-c3: fixed schedule 'segments_per_sm,warp_mask,flags' instead of autotuning")
+    ap.add_argument("--ref-budget", type=float, default=4.0,
+                    help="reference arm: seconds of CPU work per step (the sample is sized to it)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

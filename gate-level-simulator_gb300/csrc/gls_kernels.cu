@@ -254,8 +254,8 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
     }
     if (threadIdx.x <= kClasses) s_sum[threadIdx.x] = 0;
     // Pass 1: every gate output's fan-in events E and fan-in class, parked
-    // in its slot entry as E << 2 | class (and its output net in its scratch
-    // entry) until pass 2 overwrites both; the level's fan-in events per
+    // in its slot entry as E << 2 | class until pass 2 overwrites it; the
+    // level's fan-in events per
     // class (every class runs as its own launch, so every class is split
     // into about seg_target segments) and its gate events.
     const uint32_t step = blockDim.x * kPlanPer;
@@ -278,7 +278,6 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
                 for (int p = 0; p < md.n_pins; ++p) g_tot += w.net_len[md.net[(md.pin_slot >> (3 * p)) & 7u]];
             }
             w.slot[i] = (E << 2) | (unsigned long long)c;
-            w.scr[i] = md.out_net;
         }
     }
     __syncthreads();   // s_sum cleared
@@ -328,11 +327,10 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
     unsigned long long run_slot = 0, run_scr = 0;
     for (uint32_t r = 0; r < n; r += blockDim.x) {
         const uint32_t i = r + threadIdx.x;
-        uint32_t S = 0, onet = 0;
+        uint32_t S = 0;
         unsigned long long slot = 0, scr = 0;
         if (i < n) {
             const unsigned long long ec = w.slot[i];
-            onet = (uint32_t)w.scr[i];
             const unsigned long long E = ec >> 2;
             const uint32_t seg = s_seg[ec & 3u];
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
@@ -347,10 +345,8 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         block_excl_scan3(xs, xo, xc, tS, tSlot, tScr, sm32, sm64, sm64b);
         if (i < n) {
             w.seg_base[i] = run_seg + xs;
-            const unsigned long long st = base + run_slot + xo;
-            w.slot[i] = st;
+            w.slot[i] = base + run_slot + xo;
             w.scr[i] = run_scr + xc;
-            w.net_off[onet] = st;
         }
         run_seg += tS;
         run_slot += tSlot;
@@ -364,8 +360,10 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         if (run_seg > w.seg_cap) e |= kErrSegCap;
         if (run_scr > w.scr_cap) e |= kErrScratch;
         if (base + run_slot > w.cap) e |= kErrPool;
-        else *w.top = base + run_slot;
+        // the pool pointer moves only for a plan that holds: a caller that
+        // owns the pool may retry a failed level with fewer outputs
         if (e) atomicOr(w.err, e);
+        else *w.top = base + run_slot;
         s_fail = e != 0;
         atomicAdd(&w.counters[2], (unsigned long long)run_seg);
     }
@@ -1453,6 +1451,8 @@ __global__ void __launch_bounds__(256, GLS_LINK_BLOCKS) k_link(const WinSet<kBat
                 w.slot[i] = st;
             }
             w.net_off[out_net] = st;
+        } else {
+            w.net_off[out_net] = slot;   // written here, not by the plan: a failed level leaves the table as it was
         }
         // the last event holds until t_end; k_copy adds the rest
         unsigned long long acc[3] = {0, 0, 0};

@@ -33,7 +33,7 @@ constexpr uint64_t kStaticMaxWords = 4194304;        // segment-stack words per 
 
 // Layout of the static scratch (byte offsets, each 256-byte aligned).
 constexpr uint64_t al256(uint64_t x) { return (x + 255) & ~255ull; }
-constexpr uint64_t kOffSmall = 0;                                            // 8 x u64: err, counters, n_segs
+constexpr uint64_t kOffSmall = 0;   // 8 x u64: saved pool pointer, 4 counters, err, n_segs, presize overflows
 constexpr uint64_t kOffWin = 64;                                             // the level kernels' WinDev
 constexpr uint64_t kOffSegBase = al256(kOffWin + sizeof(WinDev));
 constexpr uint64_t kOffSlot = al256(kOffSegBase + 4ull * (kStaticMaxOutputs + 1));
@@ -61,9 +61,19 @@ int scratch_address(int device, unsigned char **out, std::string &err)
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_addr[device]) {
         void *p = nullptr;
+        // With lazy module loading (the CUDA default) this lookup is what
+        // loads the module and reserves the array on the device, so it can
+        // fail for lack of device memory when a caller's arena already holds
+        // all of it.
         const cudaError_t e = cudaGetSymbolAddress(&p, g_level_scratch);
         if (e != cudaSuccess) {
             err = std::string("cudaGetSymbolAddress of the static scratch failed: ") + cudaGetErrorString(e);
+            if (e == cudaErrorMemoryAllocation) {
+                cudaGetLastError();   // reset the last-error state (an allocation failure is not sticky)
+                err += " (the 20 MiB static array could not be reserved: make the first call before an arena "
+                       "takes the remaining device memory)";
+                return GLS_ENOMEM;
+            }
             return GLS_ECUDA;
         }
         g_addr[device] = static_cast<unsigned char *>(p);
@@ -91,8 +101,8 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
         return ctx_fail(ctx, GLS_EINVAL, "run_level_static: level %u out of range", level);
     const uint32_t lo = ctx->drv_level_start[level], hi = ctx->drv_level_start[level + 1];
     if ((uint64_t)first + count > hi - lo)
-        return ctx_fail(ctx, GLS_EINVAL, "run_level_static: outputs [%u, %u) outside level %u (%u outputs)", first,
-                        first + count, level, hi - lo);
+        return ctx_fail(ctx, GLS_EINVAL, "run_level_static: outputs [%u, %llu) outside level %u (%u outputs)", first,
+                        (unsigned long long)first + count, level, hi - lo);
     if (count > kStaticMaxOutputs)
         return ctx_fail(ctx, GLS_ERANGE, "run_level_static: %u gate outputs in one call; the static scratch holds %u",
                         count, kStaticMaxOutputs);
@@ -108,6 +118,11 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     // previous call's contents otherwise)
     e = cudaMemsetAsync(small, 0, 64, ctx->stream);
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "clear static flags: %s", cudaGetErrorString(e));
+    // the caller's pool pointer as it was, put back if the level fails, so
+    // that a failed call (e.g. GLS_ERANGE, retried with fewer outputs) uses
+    // up no pool space; small[0] holds it
+    e = cudaMemcpyAsync(small, d_top, 8, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "save pool pointer: %s", cudaGetErrorString(e));
     WinDev d;
     std::memset(&d, 0, sizeof d);
     d.net_off = d_net_off;
@@ -156,6 +171,11 @@ extern "C" int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first
     if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "run_level_static: %s", cudaGetErrorString(e));
     const uint32_t ef = (uint32_t)st[5];
     if (ef) {
+        // k_link and k_copy skip a failed level, so net_off, net_len and the
+        // SAIF counters are untouched; only the pool pointer may have moved
+        e = cudaMemcpyAsync(d_top, small, 8, cudaMemcpyDeviceToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return ctx_fail(ctx, GLS_ECUDA, "restore pool pointer: %s", cudaGetErrorString(e));
         if (ef & kErrScratch)
             return ctx_fail(ctx, GLS_ERANGE,
                             "run_level_static: the outputs' fan-in events need more than the %llu-word static "

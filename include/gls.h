@@ -387,12 +387,17 @@ int gls_trainer_set_params(gls_trainer *tr, const float *params);
  * until exit.  One
  * call handles at most 16384 gate outputs, 65536 time segments and
  * 4194304 segment-stack words; larger requests fail with GLS_ERANGE and a
- * message (pass fewer outputs per call).  The call waits for its kernels
- * (on the context's stream) to finish.  The first call on a device looks up
- * the static array's device address; make that first call before any
- * stream capture.  All calls on a device share the array: calls that
- * overlap on the GPU (other threads, other contexts of the same device)
- * race and must be serialized by the caller. */
+ * message (pass fewer outputs per call).  A call that fails leaves d_top,
+ * d_net_off, d_net_len and d_saif as they were, so it can be retried with
+ * fewer outputs.  The call waits for its kernels (on the context's stream)
+ * to finish.  The first call on a device looks up the static array's device
+ * address, which (with CUDA's default lazy module loading) is also when the
+ * array is reserved on that device: make that first call before any stream
+ * capture and before an arena takes the remaining device memory; if the
+ * array cannot be reserved the call fails with GLS_ENOMEM.  All calls on a
+ * device share the array: calls that overlap on the GPU (other threads,
+ * other contexts of the same device) race and must be serialized by the
+ * caller. */
 int gls_run_level_static(gls_ctx *ctx, uint32_t level, uint32_t first, uint32_t count,
                          uint32_t *d_pool, uint64_t pool_cap, unsigned long long *d_top,
                          uint64_t *d_net_off, uint32_t *d_net_len,

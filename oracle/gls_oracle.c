@@ -8,7 +8,7 @@
  *
  * Parity is pinned: tests/test_oracle.py checks this restatement against the
  * reference's own functions compiled from the reference sources
- * (oracle/build_ref.py -> oracle/_ref/ref_sim) and against the committed
+ * (oracle/build.py -> oracle/_ref/ref_sim) and against the committed
  * golden vectors in tests/golden/.
  *
  * Functions and the reference lines they restate:
@@ -28,6 +28,14 @@
  * usage: gls_oracle <case> <result> [--calc fixed|literal] [--factor F]
  *                   [--threads N] [--insts a:b]   (simulate only that
  *                   instance range; inputs must then come from stimulus)
+ *                   [--keep nets.bin]  (write the waveforms of only these
+ *                   nets: u32 count, then u32 net ids; every other net's
+ *                   list is freed after the last level that reads it, once
+ *                   its SAIF counts are taken -- a run over a large design
+ *                   then holds only the lists still to be read)
+ *                   [--verify-lookup]  (also run GetValueAt's binary search
+ *                   at every step and stop if it disagrees with the cursor
+ *                   values the simulation uses)
  *
  * Asserts of the reference are treated as compiled with NDEBUG: an input
  * edge that is neither rise nor fall counts as posedge
@@ -63,6 +71,7 @@ static Wave *g_wave;
 static uint64_t g_t_begin, g_t_end;
 static int g_literal = 0;
 static double g_factor = 1.0;
+static int g_verify_lookup = 0;
 
 static void die(const char *m) { fprintf(stderr, "gls_oracle: %s\n", m); exit(2); }
 
@@ -350,9 +359,26 @@ static void simulate_output(const Inst *in, int o, Wave *outw)
         uint32_t chg = 0;
         for (int j = 0; j < m; ++j)
             if (cursor[j] < w[j]->n && w[j]->t[cursor[j]] == t) { chg |= 1u << j; cursor[j]++; }
-        /* cur / last value of every input pin (GetValueAt) */
+        /* cur / last value of every input pin.  GetValueAt's binary search
+         * finds, for a net with an event at t, that event's value and the one
+         * before it (X for a first event), else the value of the last event
+         * before t (X if none) for both; the cursors, just moved past the
+         * events at t, give the same values directly. */
         uint8_t cur_net[16], last_net[16], pin_val[16];
-        for (int j = 0; j < m; ++j) get_value_at(w[j], t, &cur_net[j], &last_net[j]);
+        for (int j = 0; j < m; ++j) {
+            const uint64_t c = cursor[j];
+            if ((chg >> j) & 1u) {
+                cur_net[j] = w[j]->v[c - 1];
+                last_net[j] = c >= 2 ? w[j]->v[c - 2] : VX;
+            } else {
+                cur_net[j] = last_net[j] = c ? w[j]->v[c - 1] : VX;
+            }
+            if (g_verify_lookup) {
+                uint8_t vc, vl;
+                get_value_at(w[j], t, &vc, &vl);
+                if (vc != cur_net[j] || vl != last_net[j]) die("cursor values disagree with GetValueAt");
+            }
+        }
         for (int p = 0; p < cl->n_in; ++p)
             for (int j = 0; j < m; ++j) if (nets[j] == in->in[p]) pin_val[p] = cur_net[j];
         uint8_t F = run_function(cl, pin_val, o);
@@ -429,6 +455,25 @@ static void *worker(void *arg)
     return NULL;
 }
 
+/* ------------------------------------------------------ lean mode (--keep) */
+static uint8_t *g_keep;          /* per net: 1 = write its waveform */
+static int32_t *g_free_after;    /* per net: level after which its list is dropped (-1: at once) */
+static uint64_t (*g_saif)[3];    /* per net: counts taken before a list is dropped */
+static uint8_t *g_saif_done;
+
+static void saif_integral(const Wave *w, uint64_t start, uint64_t end, uint64_t r[3]);
+
+static void drop_list(uint32_t n)
+{
+    Wave *w = &g_wave[n];
+    if (!w->valid || g_saif_done[n]) return;
+    saif_integral(w, g_t_begin, g_t_end, g_saif[n]);
+    g_saif_done[n] = 1;
+    if (g_keep[n]) return;
+    free(w->t); free(w->v);
+    w->t = NULL; w->v = NULL; w->n = w->cap = 0;
+}
+
 /* ----------------------------------------------------------------- SAIF */
 static void saif_integral(const Wave *w, uint64_t start, uint64_t end, uint64_t r[3])
 {
@@ -451,21 +496,57 @@ static void saif_integral(const Wave *w, uint64_t start, uint64_t end, uint64_t 
 
 int main(int argc, char **argv)
 {
-    if (argc < 3) die("usage: gls_oracle <case> <result> [--calc fixed|literal] [--factor F] [--threads N] [--insts a:b]");
+    if (argc < 3) die("usage: gls_oracle <case> <result> [--calc fixed|literal] [--factor F] [--threads N] [--insts a:b] "
+                      "[--keep nets.bin] [--verify-lookup]");
     int threads = 1;
     long lo = -1, hi = -1;
+    const char *keep_path = NULL;
     for (int i = 3; i < argc; ++i) {
         if (!strcmp(argv[i], "--calc") && i + 1 < argc) g_literal = !strcmp(argv[++i], "literal");
         else if (!strcmp(argv[i], "--factor") && i + 1 < argc) g_factor = atof(argv[++i]);
         else if (!strcmp(argv[i], "--threads") && i + 1 < argc) threads = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--insts") && i + 1 < argc) {
             if (sscanf(argv[++i], "%ld:%ld", &lo, &hi) != 2) die("bad --insts");
-        } else die("unknown option");
+        } else if (!strcmp(argv[i], "--keep") && i + 1 < argc) keep_path = argv[++i];
+        else if (!strcmp(argv[i], "--verify-lookup")) g_verify_lookup = 1;
+        else die("unknown option");
     }
     read_case(argv[1]);
     if (threads < 1) threads = 1;
     if (lo < 0) { lo = 0; hi = g_n_inst; }
     if (hi > (long)g_n_inst) hi = g_n_inst;
+    const int lean = keep_path != NULL;
+    if (lean) {
+        g_keep = calloc(g_n_nets, 1);
+        g_free_after = malloc(sizeof(int32_t) * g_n_nets);
+        g_saif = calloc(g_n_nets, sizeof *g_saif);
+        g_saif_done = calloc(g_n_nets, 1);
+        if (!g_keep || !g_free_after || !g_saif || !g_saif_done) die("out of memory");
+        FILE *kf = fopen(keep_path, "rb");
+        if (!kf) die("cannot open --keep file");
+        uint32_t nk;
+        if (fread(&nk, 4, 1, kf) != 1) die("truncated --keep file");
+        for (uint32_t k = 0; k < nk; ++k) {
+            uint32_t n;
+            if (fread(&n, 4, 1, kf) != 1) die("truncated --keep file");
+            if (n >= g_n_nets) die("bad net in --keep file");
+            g_keep[n] = 1;
+        }
+        fclose(kf);
+        /* a list is dropped after the last level that reads it; one that no
+         * simulated instance reads, after the level that makes it */
+        for (uint32_t n = 0; n < g_n_nets; ++n) g_free_after[n] = -1;
+        for (long k = lo; k < hi; ++k) {
+            const Inst *in = &g_inst[k];
+            const Cell *cl = &g_cells[in->cell];
+            for (int q = 0; q < cl->n_in; ++q)
+                if ((int32_t)in->level > g_free_after[in->in[q]]) g_free_after[in->in[q]] = (int32_t)in->level;
+            for (int q = 0; q < cl->n_out; ++q)
+                if ((int32_t)in->level > g_free_after[in->out[q]]) g_free_after[in->out[q]] = (int32_t)in->level;
+        }
+        for (uint32_t n = 0; n < g_n_nets; ++n)
+            if (g_free_after[n] < 0) drop_list(n);
+    }
     /* level loop: instances are stored in level order */
     uint32_t i = (uint32_t)lo;
     while (i < (uint32_t)hi) {
@@ -476,6 +557,11 @@ int main(int argc, char **argv)
         int nt = threads > 256 ? 256 : threads;
         for (int k = 0; k < nt; ++k) pthread_create(&th[k], NULL, worker, NULL);
         for (int k = 0; k < nt; ++k) pthread_join(th[k], NULL);
+        if (lean) {
+            const int32_t L = (int32_t)g_inst[i].level;
+            for (uint32_t n = 0; n < g_n_nets; ++n)
+                if (g_free_after[n] == L) drop_list(n);
+        }
         i = j;
     }
     FILE *f = fopen(argv[2], "wb");
@@ -484,15 +570,17 @@ int main(int argc, char **argv)
     fwrite(&g_n_nets, 4, 1, f);
     for (uint32_t n = 0; n < g_n_nets; ++n) {
         const Wave *w = &g_wave[n];
-        uint64_t cnt = w->valid ? w->n : UINT64_MAX;
+        const int write = w->valid && (!lean || g_keep[n]);
+        uint64_t cnt = write ? w->n : UINT64_MAX;
         fwrite(&cnt, 8, 1, f);
-        if (!w->valid) continue;
+        if (!write) continue;
         fwrite(w->t, 8, w->n, f);
         fwrite(w->v, 1, w->n, f);
     }
     for (uint32_t n = 0; n < g_n_nets; ++n) {
         uint64_t r[3] = {UINT64_MAX, UINT64_MAX, UINT64_MAX};
-        if (g_wave[n].valid) saif_integral(&g_wave[n], g_t_begin, g_t_end, r);
+        if (lean && g_saif_done[n]) memcpy(r, g_saif[n], sizeof r);
+        else if (g_wave[n].valid) saif_integral(&g_wave[n], g_t_begin, g_t_end, r);
         fwrite(r, 8, 3, f);
     }
     fclose(f);

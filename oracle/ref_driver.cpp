@@ -3,7 +3,7 @@
 // Runs the reference's own serial simulator core -- SimulateInst, Process,
 // Calculate, AddDelay, CheckDelay, RunFunction, GetValueAt, calc and the CPU
 // DumpSaif of src/simulate.cpp:37-1506, compiled from the reference sources
-// by oracle/build_ref.py -- on a case file (oracle/casefile.py), with the
+// by oracle/build.py -- on a case file (oracle/casefile.py), with the
 // level loop of src/simulate.cpp:1569-1668.
 //
 // The reference's `main` does not compile against its own VCDParser, so this

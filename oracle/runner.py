@@ -25,14 +25,24 @@ def parse_saif_records(text: str) -> dict[str, tuple[int, int, int]]:
     return {m.group(1): (int(m.group(2)), int(m.group(3)), int(m.group(4))) for m in SAIF_NET.finditer(text)}
 
 
-def run_oracle(nl, st, t_begin, t_end, calc="fixed", threads=1, factor=1.0, workdir=None, **case_kw):
+def run_oracle(nl, st, t_begin, t_end, calc="fixed", threads=1, factor=1.0, workdir=None, keep=None,
+               verify_lookup=False, **case_kw):
+    """keep: only these nets' waveforms come back (every list is dropped
+    after the last level that reads it, so a large design fits in host
+    memory); SAIF counts come back for every net either way."""
     exe = build.build_oracle()
     with tempfile.TemporaryDirectory(dir=workdir) as d:
         case, res = Path(d) / "c.bin", Path(d) / "r.bin"
         write_case(case, nl, st, t_begin, t_end, **case_kw)
+        cmd = [str(exe), str(case), str(res), "--calc", calc, "--threads", str(threads), "--factor", repr(factor)]
+        if keep is not None:
+            k = np.unique(np.asarray(keep, np.uint32))
+            (Path(d) / "keep.bin").write_bytes(np.uint32(len(k)).tobytes() + k.astype("<u4").tobytes())
+            cmd += ["--keep", str(Path(d) / "keep.bin")]
+        if verify_lookup:
+            cmd += ["--verify-lookup"]
         t0 = time.perf_counter()
-        subprocess.run([str(exe), str(case), str(res), "--calc", calc, "--threads", str(threads),
-                        "--factor", repr(factor)], check=True)
+        subprocess.run(cmd, check=True)
         el = time.perf_counter() - t0
         waves, saif = read_result(res)
     return waves, saif, el

@@ -9,8 +9,10 @@ import pytest
 from gls import files, synth
 from gls.build import BIN_DIR
 from gls.cells import LIBRARY
+from oracle.build import REFERENCE
 
-REF_VLIB = Path("/root/reference/examples/GENERIC_STD_CELL.vlib")
+# the reference checkout's cell library (GLS_REFERENCE names the checkout)
+REF_VLIB = REFERENCE / "examples" / "GENERIC_STD_CELL.vlib"
 
 
 @pytest.fixture(scope="module")

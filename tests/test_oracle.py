@@ -99,3 +99,31 @@ def test_oracle_delay_factor(oracle_bin):
     st = stimulus({0: [(0, 0), (100, 3), (200, 0)]})
     w, _, _ = run_oracle(nl, st, 0, 300, factor=0.1)
     assert list(zip(w[1][0].tolist(), w[1][1].tolist())) == [(0, 1), (4, 0), (103, 3), (204, 0)]
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_oracle_cursor_values_equal_get_value_at(seed, oracle_bin):
+    """The oracle takes each step's current and previous input values from
+    its merge cursors; --verify-lookup also runs the binary search of
+    GetValueAt (src/simulate.cpp:1459-1506) at every step and stops on any
+    difference.  Random cases with X/Z, duplicate nets and repeated times
+    across nets."""
+    nl, st = random_case(6100 + seed, max_gates=30, max_in=6, horizon=2000, max_events=120, xz=True)
+    w1, s1, _ = run_oracle(nl, st, 0, 2100, verify_lookup=True)
+    assert w1
+
+
+def test_oracle_keep_mode_matches_full_run(oracle_bin):
+    """--keep drops every list after the last level that reads it: the kept
+    nets' waveforms and every net's SAIF counts equal a full run's."""
+    from gls import synth
+    cfg = synth.scaled(synth.CONFIGS["c2"], cells=3_000, cycles=300, depth=12)
+    nl = synth.make_netlist(cfg, seed=8)
+    st = synth.make_stimulus(cfg, nl.ppi_nets, seed=9)
+    full_w, full_s, _ = run_oracle(nl, st, 0, cfg.t_end, threads=4)
+    keep = np.arange(0, nl.n_nets, 97)
+    lean_w, lean_s, _ = run_oracle(nl, st, 0, cfg.t_end, threads=4, keep=keep)
+    assert set(lean_w) == {int(n) for n in keep if int(n) in full_w}
+    for n in lean_w:
+        assert np.array_equal(lean_w[n][0], full_w[n][0]) and np.array_equal(lean_w[n][1], full_w[n][1])
+    assert np.array_equal(lean_s, full_s)
