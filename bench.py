@@ -340,9 +340,9 @@ def gls_arm(args):
                 cache[n] = sim.waveform(int(n), 0)
             return cache[n]
 
-        from oracle.sample import sample_order, sized_sample
+        from oracle.sample import run_sample, sample_order
         t0 = time.time()
-        cpu = sized_sample(nl, waves_of, cfg.t_end, os.cpu_count() or 1, sample_order(nl), 8.0)
+        cpu = run_sample(nl, waves_of, sample_order(nl)[: args.parity_gates], 0, cfg.t_end, os.cpu_count() or 1)
         parity = parity_check(sim, cpu)
         log(f"parity sample: {parity['gates_checked']} gates, {parity['mismatches']} mismatches "
             f"({time.time() - t0:.1f}s)")
@@ -570,6 +570,8 @@ def main():
     ap.add_argument("--windows", type=int, default=None, help="c4: number of windows (default 256)")
     ap.add_argument("--schedule", default=None,
                     help="c1-c3: fixed schedule 'segments_per_sm,warp_mask,flags' instead of autotuning")
+    ap.add_argument("--parity-gates", type=int, default=2000,
+                    help="gates of the sample checked against the reference core (and timed as the CPU baseline)")
     ap.add_argument("--ref-budget", type=float, default=4.0,
                     help="reference arm: seconds of CPU work per step (the sample is sized to it)")
     args = ap.parse_args()

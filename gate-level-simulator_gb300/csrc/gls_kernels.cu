@@ -423,6 +423,9 @@ __device__ __forceinline__ uint32_t sel4(const uint4 &q, uint32_t k)
 #ifndef GLS_READER_W2
 #define GLS_READER_W2 2   // events per reader chunk in the 1- and 2-input gate kernels
 #endif
+#ifndef GLS_SIM_WARP_BATCH
+#define GLS_SIM_WARP_BATCH 1   // thread-per-segment kernels: a warp takes 32 segments at a time
+#endif
 #ifndef GLS_READER_W3
 #define GLS_READER_W3 1   // events per reader chunk in the wider gate kernels
 #endif
@@ -795,9 +798,26 @@ __global__ void __launch_bounds__(128, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_
     __shared__ uint32_t s_hint;   // a driver near the block's latest segment
     if (threadIdx.x == 0) { s_next = b0; s_hint = d0; }
     __syncthreads();
+#if GLS_SIM_WARP_BATCH
+    // A warp takes 32 consecutive segments at a time, one per lane, so that
+    // its lanes start (cut searches), walk and finish their segments
+    // together: the segments of one gate output hold equal shares of its
+    // two longest input lists.  Lanes that took segments one by one drift
+    // apart, and then a segment's setup runs on one lane while the others
+    // walk events, each path issued for the few lanes on it.
+    const uint32_t lane_id = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t qb = 0;
+        if (lane_id == 0) qb = atomicAdd(&s_next, 32u);
+        qb = __shfl_sync(0xffffffffu, qb, 0);
+        if (qb >= b1) break;
+        const uint32_t q = qb + lane_id;
+        if (q >= b1) continue;
+#else
     for (;;) {
         const uint32_t q = atomicAdd(&s_next, 1u);
         if (q >= b1) break;
+#endif
         const uint32_t win = kBatch ? window_of(s_pre, nwin, q) : 0u;
         const WinDev &w = ws.get(win);
         const uint32_t g = kBatch ? q - s_pre[win] + w.seg_base[d0] : q;

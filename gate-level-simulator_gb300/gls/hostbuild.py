@@ -10,8 +10,8 @@ from .build import BIN_DIR, LIB, LIB_DIR, PKG, REPO
 
 HOST = PKG / "host"
 TOOLS = {
-    "gls_process": ["design.cpp", "gls_process.cpp"],
-    "gls_simulate": ["design.cpp", "vcd.cpp", "gls_simulate.cpp"],
+    "gls_process": ["design.cpp", "boost_inter.cpp", "gls_process.cpp"],
+    "gls_simulate": ["design.cpp", "boost_inter.cpp", "vcd.cpp", "gls_simulate.cpp"],
 }
 
 

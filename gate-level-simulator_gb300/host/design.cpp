@@ -6,6 +6,7 @@
 // 1276-1464), written as a small tokenizer instead of line splitting, so a
 // statement may span lines and carry comments.
 #include "design.h"
+#include "boost_inter.h"
 
 #include <algorithm>
 #include <cctype>
@@ -236,17 +237,25 @@ bool parse_vlib(const std::string &text, Library &lib, std::string *err)
             if (k == "input" || k == "output" || k == "inout" || k == "wire" || k == "reg" || k == "supply0" ||
                 k == "supply1") {
                 size_t a = 1;
-                if (a < st.size() && st[a] == "[") {   // ranges are not used by the cells
+                int l = -1, r = -1;
+                if (a < st.size() && st[a] == "[") {   // ranges are not used by the cells, only recorded
+                    if (a + 3 < st.size()) {
+                        l = atoi(st[a + 1].c_str());
+                        r = st[a + 2] == ":" ? atoi(st[a + 3].c_str()) : l;
+                    }
                     while (a < st.size() && st[a] != "]") ++a;
                     ++a;
                 }
+                if (k == "supply0") m.cell.sup0_tokens.push_back(k);
+                if (k == "supply1") m.cell.sup1_tokens.push_back(k);
                 for (; a < st.size(); ++a) {
                     if (st[a] == ",") continue;
                     if (k == "input") m.cell.inputs.push_back(st[a]);
                     else if (k == "output") m.cell.outputs.push_back(st[a]);
                     else if (k == "inout") m.cell.inputs.push_back(st[a]);
-                    else if (k == "supply0") m.sup0.insert(st[a]);
-                    else if (k == "supply1") m.sup1.insert(st[a]);
+                    else if (k == "supply0") { m.sup0.insert(st[a]); m.cell.sup0_tokens.push_back(st[a]); }
+                    else if (k == "supply1") { m.sup1.insert(st[a]); m.cell.sup1_tokens.push_back(st[a]); }
+                    if (k != "supply0" && k != "supply1") m.cell.decls.push_back({st[a], k, l, r});
                 }
                 continue;
             }
@@ -271,6 +280,7 @@ bool parse_vlib(const std::string &text, Library &lib, std::string *err)
                 p.out = args[0];
                 p.ins.assign(args.begin() + 1, args.end());
                 m.prims.push_back(p);
+                m.cell.funcs.push_back({k, f, p.ins, p.out});
                 continue;
             }
             // other statements (instances of unknown UDPs, tables, ...) are ignored
@@ -347,6 +357,7 @@ bool parse_gv(const std::string &text, const Library &lib, Design &d, std::strin
     d.constants.push_back({c1, 3});
     bool in_module = false;
     std::set<std::string> ignored(lib.ignored.begin(), lib.ignored.end());
+    d.ignored = lib.ignored;
     while (statement(L, st)) {
         if (st.empty()) continue;
         const std::string &k = st[0];
@@ -367,6 +378,7 @@ bool parse_gv(const std::string &text, const Library &lib, Design &d, std::strin
             }
             for (; a < st.size(); ++a) {
                 if (st[a] == ",") continue;
+                d.decls.push_back({st[a], k, l, r});
                 if (l >= 0) {
                     ranges[st[a]] = {l, r};
                     for (int b = l;; b += (r > l ? 1 : -1)) {
@@ -396,6 +408,7 @@ bool parse_gv(const std::string &text, const Library &lib, Design &d, std::strin
                 if (rhs[b] == "1'b0") d.constants.push_back({ln, 0});
                 else if (rhs[b] == "1'b1") d.constants.push_back({ln, 3});
                 else d.aliases.push_back({ln, d.net(rhs[b])});
+                if (rhs[b] == "1'b0" || rhs[b] == "1'b1") d.assign_consts.push_back(ln);
             }
             continue;
         }
@@ -409,6 +422,7 @@ bool parse_gv(const std::string &text, const Library &lib, Design &d, std::strin
         const Cell &cell = lib.cells[lit->second];
         Instance in;
         in.name = st[1];
+        in.gv_index = (uint32_t)d.insts.size();
         auto dc = design_cell.find(cell.name);
         if (dc == design_cell.end()) {
             dc = design_cell.emplace(cell.name, (uint32_t)d.cells.size()).first;
@@ -456,6 +470,7 @@ bool parse_gv(const std::string &text, const Library &lib, Design &d, std::strin
             }
             if (bits.empty()) continue;   // .port() left open
             pins[p] = (int)d.net(bits[0]);
+            in.conn.push_back((uint32_t)p);
         }
         for (size_t p = 0; p < pins.size(); ++p) {
             if (pins[p] >= 0) continue;
@@ -835,8 +850,12 @@ bool read_inter(const std::string &path, Design &d, std::string *err)
         if (err) *err = e2.empty() ? "empty " + path : e2;
         return false;
     }
+    if (is_boost_text_archive(b)) {   // the reference's own format
+        ref::Inter in;
+        return load_boost_inter(b, in, err) && ref_inter_to_design(in, d, err);
+    }
     if (b.compare(0, 8, "GLSINTR1") != 0) {
-        if (err) *err = path + " is not a gls inter.dat (a Boost text archive of the reference is not read)";
+        if (err) *err = path + " is neither a gls inter.dat nor a Boost text archive";
         return false;
     }
     R r(b);

@@ -28,6 +28,24 @@ struct Cell {
         std::vector<uint8_t> pins;   // inputs, then the driven pin
     };
     std::vector<Prim> prims;
+    // What the reference's ModuleType also records (kept for the Boost
+    // inter.dat writer): every input / output / inout / wire / reg
+    // declaration, the supply statements' tokens as its parser keeps them
+    // (the keyword first, src/PreProcess.cpp:614-629) and the primitives by
+    // port name.
+    struct Decl {
+        std::string name, type;
+        int l = -1, r = -1;   // bus range, -1 for a scalar
+    };
+    std::vector<Decl> decls;
+    std::vector<std::string> sup0_tokens, sup1_tokens;
+    struct Func {
+        std::string name;   // and, or, ..., udp_xbuf, udp_mux2
+        int id;             // GLS_F_*
+        std::vector<std::string> ins;
+        std::string out;
+    };
+    std::vector<Func> funcs;
 };
 
 struct Arc {
@@ -42,6 +60,8 @@ struct Instance {
     uint32_t cell;
     std::vector<uint32_t> pins;   // input nets then output nets (net ids)
     std::vector<Arc> arcs;
+    uint32_t gv_index = 0;        // position in the netlist file (the reference's instance id)
+    std::vector<uint32_t> conn;   // connected cell ports (pin indexes) in the order the netlist lists them
 };
 
 struct Design {
@@ -54,6 +74,9 @@ struct Design {
     std::vector<std::pair<uint32_t, uint8_t>> constants;   // net, value (0 or 3)
     std::vector<std::pair<uint32_t, uint32_t>> aliases;    // assign left <- right
     std::vector<uint32_t> bus_bits;           // declared bus bits (reported even when undriven)
+    std::vector<Cell::Decl> decls;            // the netlist's input / output / wire / inout declarations
+    std::vector<std::string> ignored;         // library modules the front end skips
+    std::vector<uint32_t> assign_consts;      // nets an assign ties to 1'b0 / 1'b1
 
     uint32_t net(const std::string &name);    // id of a net, created on first use
     int find_net(const std::string &name) const;
@@ -80,6 +103,7 @@ bool levelize(Design &d, std::string *err);
 void instance_preds(const Design &d, std::vector<uint64_t> &start, std::vector<uint32_t> &pred);
 void apply_levels(Design &d, const std::vector<uint32_t> &order, const std::vector<uint32_t> &level_start);
 bool write_inter(const std::string &path, const Design &d, std::string *err);
+// Reads either format: the native one or the reference's Boost text archive.
 bool read_inter(const std::string &path, Design &d, std::string *err);
 
 }  // namespace glsh

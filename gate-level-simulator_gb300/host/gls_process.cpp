@@ -1,24 +1,35 @@
-// gls_process [--gpu-levelize] <vlib> <gv> <sdf> <inter.dat>
+// gls_process [--gpu-levelize] [--native] <vlib> <gv> <sdf> <inter.dat>
 //
 // The `process` step of the reference (src/process.cpp:178-610): read the
 // Verilog cell library, the flat gate-level netlist and the SDF file,
 // levelize the instance graph and write the levelized design to inter.dat
-// (native binary format; see host/design.cpp).  With --gpu-levelize the
-// levels are computed on GPU 0 (gls_levelize); the file is the same.
+// as the reference does, a Boost text archive of its `inter` class
+// (host/boost_inter.cpp); --native writes the tools' own binary format
+// instead (host/design.cpp).  With --gpu-levelize the levels are computed
+// on GPU 0 (gls_levelize); the file is the same.
 #include <cstdio>
+#include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
+#include "boost_inter.h"
 #include "design.h"
 #include "gls.h"
 
 int main(int argc, char **argv)
 {
-    const bool gpu = argc == 6 && std::string(argv[1]) == "--gpu-levelize";
-    if (gpu) ++argv, --argc;
-    if (argc != 5) {
-        printf("[USAGE] ./gls_process vlib_path gv_path sdf_path intermediate_file\n");
+    bool gpu = false, native = false;
+    std::vector<char *> pos;
+    for (int k = 1; k < argc; ++k) {
+        if (!strcmp(argv[k], "--gpu-levelize")) gpu = true;
+        else if (!strcmp(argv[k], "--native")) native = true;
+        else pos.push_back(argv[k]);
+    }
+    if (pos.size() != 4) {
+        printf("[USAGE] ./gls_process [--gpu-levelize] [--native] vlib_path gv_path sdf_path intermediate_file\n");
         return 255;
     }
+    argv = pos.data() - 1;
     using namespace glsh;
     std::string err;
     Library lib;
@@ -65,9 +76,21 @@ int main(int argc, char **argv)
         return 255;
     }
     printf("levels size: %zu\n", d.level_start.size() - 1);
-    if (!write_inter(argv[4], d, &err)) {
-        printf("ERROR: %s\n", err.c_str());
-        return 255;
+    if (native) {
+        if (!write_inter(argv[4], d, &err)) {
+            printf("ERROR: %s\n", err.c_str());
+            return 255;
+        }
+    } else {
+        ref::Inter in;
+        design_to_ref_inter(d, lib, in);
+        std::ofstream f(argv[4], std::ios::binary);
+        const std::string text = save_boost_inter(in);
+        f.write(text.data(), (std::streamsize)text.size());
+        if (!f) {
+            printf("ERROR: cannot write %s\n", argv[4]);
+            return 255;
+        }
     }
     printf("store database into %s\n", argv[4]);
     return 0;

@@ -1,15 +1,19 @@
 // gls_simulate <inter.dat> <vcd> <dumpon_time> <dumpoff_time> <out.saif>
 //              [--calc fixed|literal] [--device N] [--host-vcd]
+//              [--saif-order=ref|net]
 //
 // The `simulate` step of the reference (src/simulate.cu:1786-3315) on
-// libgls: read the levelized design and the VCD stimulus, simulate every
-// level on the GPU, write T0 / T1 / TX of every net over
-// [dumpon_time, dumpoff_time) as SAIF.  Times are in the VCD time unit.
+// libgls: read the levelized design (the reference's Boost text archive or
+// the tools' native inter.dat) and the VCD stimulus, simulate every level on
+// the GPU, write T0 / T1 / TX of every net over [dumpon_time, dumpoff_time)
+// as SAIF.  Times are in the VCD time unit.
 //
 // Net coverage follows the reference GPU tool: nets read by gates and VCD
 // nets, gate outputs, constants, assign aliases (with their source's
-// counts) and declared bus bits nothing drives (all X).  Records are written
-// in net order; the reference writes them in hash-map order.
+// counts) and declared bus bits nothing drives (all X).  By default records
+// are written in net order; --saif-order=ref writes them in the order (and
+// with the coverage and ending) of the reference GPU tool, whose hash
+// containers it replays (host/boost_inter.cpp, saif_ref_order).
 //
 // The VCD body is scanned on the GPU (gls_vcd_scan) unless --host-vcd is
 // given; both read the same changes.
@@ -19,11 +23,40 @@
 #include <fstream>
 #include <string>
 #include <vector>
+#include "boost_inter.h"
 #include "design.h"
 #include "gls.h"
 #include "vcd.h"
 
 using namespace glsh;
+
+namespace {
+
+// T0 / T1 / TX of a change list over (start, end] from X, as the reference
+// integrates a VCD signal (src/simulate.cu:265-330)
+void saif_of_changes(const std::vector<uint64_t> &t, const std::vector<uint8_t> &v, uint64_t start, uint64_t end,
+                     uint64_t c[3])
+{
+    uint64_t acc[4] = {0, 0, 0, 0};   // by value: 0, X, Z, 1
+    uint64_t last = start;
+    uint8_t state = 1;
+    for (size_t k = 0; k < t.size(); ++k) {
+        if (t[k] <= start) {
+            state = v[k];
+            continue;
+        }
+        if (t[k] > end) break;
+        acc[state & 3] += t[k] - last;
+        last = t[k];
+        state = v[k];
+    }
+    if (last < end) acc[state & 3] += end - last;
+    c[0] = acc[0];
+    c[1] = acc[3];
+    c[2] = acc[1] + acc[2];
+}
+
+}  // namespace
 
 int main(int argc, char **argv)
 {
@@ -32,11 +65,13 @@ int main(int argc, char **argv)
         return 255;
     }
     int calc = GLS_CALC_FIXED, device = 0;
-    bool host_vcd = false;
+    bool host_vcd = false, ref_order = false;
     for (int k = 6; k < argc; ++k) {
         if (!strcmp(argv[k], "--calc") && k + 1 < argc) calc = !strcmp(argv[++k], "literal") ? GLS_CALC_LITERAL : GLS_CALC_FIXED;
         else if (!strcmp(argv[k], "--device") && k + 1 < argc) device = atoi(argv[++k]);
         else if (!strcmp(argv[k], "--host-vcd")) host_vcd = true;
+        else if (!strcmp(argv[k], "--saif-order=ref")) ref_order = true;
+        else if (!strcmp(argv[k], "--saif-order=net")) ref_order = false;
     }
     std::ofstream outf(argv[5]);
     if (!outf) {
@@ -50,9 +85,20 @@ int main(int argc, char **argv)
     }
     std::string err;
     Design d;
-    if (!read_inter(argv[1], d, &err)) {
-        printf("ERROR: %s\n", err.c_str());
-        return 255;
+    ref::Inter archived;   // the reference's content of the design (for --saif-order=ref)
+    {
+        const std::string bytes = read_file(argv[1], &err);
+        bool ok;
+        if (is_boost_text_archive(bytes)) {
+            ok = load_boost_inter(bytes, archived, &err) && ref_inter_to_design(archived, d, &err);
+        } else {
+            ok = read_inter(argv[1], d, &err);
+            if (ok && ref_order) design_to_ref_inter(d, Library(), archived);
+        }
+        if (!ok) {
+            printf("ERROR: %s\n", err.c_str());
+            return 255;
+        }
     }
     VcdData vcd;
     const std::string vtext = read_file(argv[2], &err);
@@ -189,6 +235,45 @@ int main(int argc, char **argv)
     auto rec = [&](const std::string &name, uint64_t a, uint64_t b, uint64_t c, const char *ind) {
         outf << ind << "(" << name << "\n" << ind << "   (T0 " << a << ") (T1 " << b << ") (TX " << c << ")\n" << ind << ")\n";
     };
+    if (ref_order) {
+        // the records in the reference GPU tool's order and coverage: nets
+        // as levels first read them, constants, unread gate outputs, unread
+        // VCD signals (their counts from the VCD itself when the design has
+        // no such net), assign aliases, then undriven declared bus bits; the
+        // file ends after the NET list, as the reference's does
+        VcdDecls decls;
+        decls.bits = vcd.decl_bits;
+        for (const SaifRecord &r : saif_ref_order(archived, decls)) {
+            if (r.kind == SaifRecord::kConst) {
+                rec(r.name, r.t0 ? dur : 0, r.t1 ? dur : 0, 0, "      ");
+                continue;
+            }
+            if (r.kind == SaifRecord::kUndriven) {
+                rec(r.name, 0, 0, dur, "      ");
+                continue;
+            }
+            const int id = r.source.empty() ? -1 : d.find_net(r.source);
+            if (id >= 0 && t0[resolve((uint32_t)id)] != UINT64_MAX) {
+                const uint32_t s = resolve((uint32_t)id);
+                rec(r.name, t0[s], t1[s], tx[s], "      ");
+                continue;
+            }
+            auto v = r.source.empty() ? vcd.index.end() : vcd.index.find(r.source);
+            if (v != vcd.index.end()) {
+                uint64_t c[3];
+                saif_of_changes(vcd.times[v->second], vcd.values[v->second], t_begin, t_end, c);
+                rec(r.name, c[0], c[1], c[2], "      ");
+                continue;
+            }
+            outf << "      (" << r.name << "\n      )\n";   // the reference prints no counts here
+        }
+        outf << "   )\n";
+        outf.close();
+        printf("simulated %zu instances in %zu levels: %llu gate-events, %llu output events, %.3f ms on the GPU\n",
+               d.insts.size(), d.level_start.size() - 1, (unsigned long long)stats.gate_events,
+               (unsigned long long)stats.output_events, stats.kernel_ms);
+        return 0;
+    }
     std::vector<uint8_t> done(n_nets, 0);
     std::vector<uint32_t> nested;   // unconnected outputs named inst[port]
     for (uint32_t n = 0; n < n_nets; ++n) {

@@ -128,6 +128,7 @@ bool parse_header(Tok &tk, VcdData &v, Vars &vars, std::string *err)
                     if (b == r) break;
                 }
             }
+            for (size_t b : var.bits) v.decl_bits.push_back({v.names[b], var.bus});
             vars[id].push_back(var);
             continue;
         }

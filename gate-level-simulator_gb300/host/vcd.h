@@ -18,6 +18,10 @@ struct VcdData {
     std::vector<std::string> names;
     std::vector<std::vector<uint64_t>> times;
     std::vector<std::vector<uint8_t>> values;        // 0, 1=X, 2=Z, 3
+    // every declared bit in $var order, and whether its declaration is a bus
+    // (the insertion order of the reference reader's InMaps_bus / InMaps_bit,
+    // src/VCDParser.cpp:283-457)
+    std::vector<std::pair<std::string, bool>> decl_bits;
 };
 
 bool parse_vcd(const std::string &text, VcdData &v, std::string *err);

@@ -33,8 +33,9 @@ def design(tmp_path_factory):
 
 
 def process(tools, d, vlib, out="inter.dat"):
-    r = subprocess.run([str(tools["gls_process"]), str(vlib), str(d / "d.gv"), str(d / "d.sdf"), str(d / out)],
-                       capture_output=True, text=True)
+    """gls_process writing the native inter.dat, which these tests read in Python."""
+    r = subprocess.run([str(tools["gls_process"]), "--native", str(vlib), str(d / "d.gv"), str(d / "d.sdf"),
+                        str(d / out)], capture_output=True, text=True)
     return r
 
 
@@ -99,7 +100,7 @@ def test_sdf_timescale_and_edges(tools, tmp_path):
         '(DELAYFILE (TIMESCALE 1ns)\n (CELL (CELLTYPE "GEN_XOR2_D1") (INSTANCE U0)\n'
         '  (DELAY (ABSOLUTE (IOPATH (posedge a1) z (0.01:0.02:0.03) (0.04:0.05:0.06))\n'
         '   (IOPATH (negedge a1) z (0.007::0.009) (0.008))\n   (IOPATH a2 z (0.1:0.1:0.1))))))\n')
-    r = subprocess.run([str(tools["gls_process"]), str(tmp_path / "lib.vlib"), str(tmp_path / "d.gv"),
+    r = subprocess.run([str(tools["gls_process"]), "--native", str(tmp_path / "lib.vlib"), str(tmp_path / "d.gv"),
                         str(tmp_path / "d.sdf"), str(tmp_path / "x.dat")], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
     arcs = files.read_inter(tmp_path / "x.dat")["insts"][0][3]

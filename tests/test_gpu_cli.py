@@ -20,8 +20,10 @@ def tools(libgls):
 
 
 def run_cli(tools, d, t_begin, t_end, extra=()):
-    r = subprocess.run([str(tools["gls_process"]), str(d / "lib.vlib"), str(d / "d.gv"), str(d / "d.sdf"),
-                        str(d / "inter.dat")], capture_output=True, text=True)
+    """gls_process (native inter.dat, which oracle_records reads in Python),
+    then gls_simulate."""
+    r = subprocess.run([str(tools["gls_process"]), "--native", str(d / "lib.vlib"), str(d / "d.gv"),
+                        str(d / "d.sdf"), str(d / "inter.dat")], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
     r = subprocess.run([str(tools["gls_simulate"]), str(d / "inter.dat"), str(d / "d.vcd"), str(t_begin),
                         str(t_end), str(d / "out.saif"), *extra], capture_output=True, text=True)
@@ -176,3 +178,76 @@ def test_cli_buses_aliases_constants(tools, tmp_path):
     assert recs["o[1]"] == (0, 0, 950)             # declared, never driven: all X
     assert recs["k0"] == (0, 950, 0)               # constant 1
     assert recs["U5[zn]"] == tuple(int(v) for v in saif[nid["U5[zn]"]])   # unconnected output
+
+
+def simulate(tools, inter, vcd, t_begin, t_end, out, extra=()):
+    r = subprocess.run([str(tools["gls_simulate"]), str(inter), str(vcd), str(t_begin), str(t_end), str(out),
+                        *extra], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return out.read_text()
+
+
+def record_names(text):
+    """NET record names of a flat SAIF file, in file order."""
+    import re
+    lines = text.splitlines()
+    return [lines[k - 1].strip()[1:] for k, x in enumerate(lines) if re.match(r"\s*\(T0 \d+\)", x)]
+
+
+def test_cli_reference_archive_and_saif_order(tools, tmp_path):
+    """The reference's inter.dat (gls_process's default Boost text archive)
+    simulates to the same SAIF as the native file; --saif-order=ref writes
+    every record once, in the reference GPU tool's order and coverage (no
+    nested instance records, the file ends after the NET list)."""
+    files.write_vlib(tmp_path / "lib.vlib")
+    (tmp_path / "d.gv").write_text(GV)
+    (tmp_path / "d.sdf").write_text(SDF)
+    (tmp_path / "d.vcd").write_text(VCD)
+    for extra, name in (([], "a.dat"), (["--native"], "n.dat")):
+        r = subprocess.run([str(tools["gls_process"]), *extra, str(tmp_path / "lib.vlib"), str(tmp_path / "d.gv"),
+                            str(tmp_path / "d.sdf"), str(tmp_path / name)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout
+    assert (tmp_path / "a.dat").read_text().startswith("22 serialization::archive ")
+    a = simulate(tools, tmp_path / "a.dat", tmp_path / "d.vcd", 50, 1000, tmp_path / "a.saif")
+    n = simulate(tools, tmp_path / "n.dat", tmp_path / "d.vcd", 50, 1000, tmp_path / "n.saif")
+    assert files.parse_saif(a) == files.parse_saif(n)
+    r = simulate(tools, tmp_path / "a.dat", tmp_path / "d.vcd", 50, 1000, tmp_path / "r.saif", ["--saif-order=ref"])
+    names = record_names(r)
+    assert len(names) == len(set(names)), "a record printed twice"
+    ref = files.parse_saif(r)
+    flat = {k: v for k, v in files.parse_saif(a).items() if k != "U5[zn]"}   # the open output has no ref record
+    assert ref == flat
+    assert r.endswith("   )\n") and "INSTANCE U5" not in r
+    # the reference order: nets as levels first read them, then constants,
+    # unread gate outputs, unread VCD signals, aliases, undriven bus bits
+    assert names.index("k0") > max(names.index(x) for x in ("a[0]", "a[1]", "w[1]"))
+    assert names[-1] == "o[1]"
+    # the same order from the native file
+    r2 = simulate(tools, tmp_path / "n.dat", tmp_path / "d.vcd", 50, 1000, tmp_path / "r2.saif", ["--saif-order=ref"])
+    assert record_names(r2) == names
+
+
+def test_cli_hand_written_archive_matches_oracle(tools, tmp_path):
+    """tests/golden/inter_small.dat (the reference's format, written by hand)
+    simulates to oracle-identical SAIF: U1 = not(a) -> n1, U2 = nand(n1, k)
+    -> y with k tied to 1, z an alias of n1, bus[1:0] undriven."""
+    from pathlib import Path
+
+    from gls.levelize import assemble
+    gold = Path(__file__).resolve().parent / "golden" / "inter_small.dat"
+    (tmp_path / "s.vcd").write_text("$timescale 1ps $end\n$scope module top $end\n$var wire 1 ! a $end\n"
+                                    "$upscope $end\n$enddefinitions $end\n#0\n0!\n#100\n1!\n#104\n0!\n"
+                                    "#300\n1!\n#700\nx!\n#800\n0!\n")
+    text = simulate(tools, gold, tmp_path / "s.vcd", 0, 1000, tmp_path / "s.saif")
+    recs = files.parse_saif(text)
+    # the oracle on the same design: nets a=0, k=1, n1=2, y=3
+    nl = assemble([("GEN_INV_D1", [0], [2], [(2, "i", "zn", 7, 9)]),
+                   ("GEN_NAND2_D1", [2, 1], [3], [(2, "a1", "zn", 11, 13), (2, "a2", "zn", 15, 17)])], n_nets=4)
+    st = stimulus({0: [(0, 0), (100, 3), (104, 0), (300, 3), (700, 1), (800, 0)], 1: [(0, 3)]})
+    ow, osaif, _ = run_oracle(nl, st, 0, 1000)
+    for name, n in (("a", 0), ("n1", 2), ("y", 3)):
+        assert recs[name] == tuple(int(x) for x in osaif[n]), name
+    assert recs["k"] == (0, 1000, 0)
+    assert recs["z"] == recs["n1"]
+    assert recs["bus[1]"] == recs["bus[0]"] == (0, 0, 1000)
+    assert set(recs) == {"a", "n1", "y", "k", "z", "bus[1]", "bus[0]"}
