@@ -69,7 +69,9 @@ endprimitive
     Path(path).write_text("`timescale 1ps/1ps\n" + udps + "\n".join(_verilog_cell(c) for c in cells) + "\n")
 
 
-def write_gv(path, nl: Netlist, top: str = "top") -> None:
+def write_gv(path, nl: Netlist, top: str = "top", order=None) -> None:
+    """The netlist as a flat gate-level Verilog file; `order` lists the
+    instances in the order to write them (default: instance order)."""
     n_reg = int(nl.extra.get("n_reg", 0))
     ppi = [int(x) for x in nl.ppi_nets]
     regs = ppi[len(ppi) - n_reg:] if n_reg else []
@@ -85,7 +87,7 @@ def write_gv(path, nl: Netlist, top: str = "top") -> None:
     for k, q in enumerate(regs):
         d = nl.net_name(gate_outs[k % len(gate_outs)]) if gate_outs else "clk"
         out.append(f"GEN_DF_D1 R{k} ( .d({d}), .cp(clk), .q({nl.net_name(q)}) );")
-    for i in range(nl.n_inst):
+    for i in (range(nl.n_inst) if order is None else (int(x) for x in order)):
         c = nl.cells[int(nl.inst_cell[i])]
         ins, outs = nl.inputs_of(i), nl.outputs_of(i)
         conns = [f".{p}({nl.net_name(int(n))})" for p, n in zip(c.inputs, ins)]

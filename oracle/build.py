@@ -1,7 +1,13 @@
-"""TEST INFRASTRUCTURE ONLY: build the two CPU oracles.
+"""TEST INFRASTRUCTURE ONLY: build the CPU oracles.
 
 1. oracle/_build/gls_oracle -- the C restatement (oracle/gls_oracle.c).
 2. oracle/_ref/ref_sim      -- the reference's own serial simulator core.
+3. oracle/_ref/ref_levels   -- the reference's levelization (GenerateAdjacencyList,
+   SetInDegrees, TopologyOrder: src/process.cpp, from the second declaration
+   of GenerateAdjacencyList, its definition, up to `main`) with
+   oracle/ref_levels_driver.cpp.
+4. oracle/_ref/ref_vcd      -- the reference's VCD reader (src/VCDParser.cpp and
+   src/VCDValue.cpp as they are) with oracle/ref_vcd_driver.cpp.
    Recipe: take src/simulate.cpp of the reference up to its `main` (which
    does not compile against the shipped VCDParser), rename its `calc` so
    oracle/ref_driver.cpp can choose the calc mode, and compile it with the
@@ -23,10 +29,13 @@ BUILD = ORACLE / "_build"
 REF = ORACLE / "_ref"
 REF_SRC = REF / "src"
 REFERENCE = Path(os.environ.get("GLS_REFERENCE", "/root/reference"))
-REF_HEADERS = ["VCDTypes.h", "Function.h", "Instance.h", "PreProcess.h", "VCDValue.h"]
+REF_HEADERS = ["VCDTypes.h", "Function.h", "Instance.h", "PreProcess.h", "VCDValue.h", "VCDParser.h"]
+REF_SOURCES = ["VCDParser.cpp", "VCDValue.cpp"]
 
 ORACLE_BIN = BUILD / "gls_oracle"
 REF_BIN = REF / "ref_sim"
+REF_LEVELS_BIN = REF / "ref_levels"
+REF_VCD_BIN = REF / "ref_vcd"
 
 
 def _run(cmd):
@@ -56,7 +65,15 @@ def extract_reference() -> bool:
     if n != 1:
         raise RuntimeError("reference calc definition not found")
     (REF_SRC / "ref_core.cpp").write_text(core)
-    for h in REF_HEADERS:
+    proc = (REFERENCE / "src" / "process.cpp").read_text()
+    decl = "void GenerateAdjacencyList("
+    first = proc.index(decl)
+    body = proc.index(decl, first + len(decl))   # the definition follows the declarations
+    levels = proc[body: proc.index("\nint main(")]
+    (REF_SRC / "ref_levels_core.cpp").write_text(
+        "#include <algorithm>\n#include <map>\n#include <string>\n#include <vector>\n#include \"Instance.h\"\n"
+        "using namespace std;\n" + levels)
+    for h in REF_HEADERS + REF_SOURCES:
         shutil.copyfile(REFERENCE / "src" / h, REF_SRC / h)
     return True
 
@@ -73,7 +90,18 @@ def build_reference(force: bool = False) -> Path | None:
         _run(["g++", "-O2", "-std=c++17", "-DNDEBUG", "-pthread", "-w",
               f"-I{ORACLE / 'ref_shim'}", f"-I{ORACLE / 'boost_stub'}", f"-I{REF_SRC}",
               "-o", str(REF_BIN), str(REF_SRC / "ref_core.cpp"), str(ORACLE / "ref_driver.cpp")])
+    _build_ref_tool(REF_LEVELS_BIN, [REF_SRC / "ref_levels_core.cpp", ORACLE / "ref_levels_driver.cpp"], force)
+    _build_ref_tool(REF_VCD_BIN, [REF_SRC / "VCDParser.cpp", REF_SRC / "VCDValue.cpp", ORACLE / "ref_vcd_driver.cpp"],
+                    force)
     return REF_BIN
+
+
+def _build_ref_tool(exe: Path, srcs: list[Path], force: bool):
+    if not all(p.exists() for p in srcs):
+        return
+    if force or not exe.exists() or any(exe.stat().st_mtime < p.stat().st_mtime for p in srcs):
+        _run(["g++", "-O2", "-std=c++17", "-DNDEBUG", "-pthread", "-w", f"-I{ORACLE / 'boost_stub'}", f"-I{REF_SRC}",
+              "-o", str(exe), *map(str, srcs)])
 
 
 def build_all(force: bool = False):

@@ -50,3 +50,45 @@ def random_case(seed: int, max_gates: int = 12, max_in: int = 4, horizon: int = 
         vs = rng.choice([0, 1, 2, 3], size=len(ts), p=probs)
         d[int(net)] = list(zip(ts.tolist(), vs.tolist()))
     return nl, stimulus(d)
+
+
+def standard_vcd(seed: int, n_scalar: int = 12, n_bus: int = 5, n_times: int = 1500) -> str:
+    """A VCD as simulators write it, in the subset the reference's reader
+    (src/VCDParser.cpp) handles: distinct identifier codes, every change on
+    its own line, full-width bus values, one change per signal and time,
+    one value per signal at time 0 (in $dumpvars), and enough timestamps
+    (> 2 x cores squared) for the reader's chunking of the body by "\\n#"."""
+    rng = np.random.default_rng(seed)
+    code = lambda k: "".join(chr(33 + d) for d in ([k % 94] if k < 94 else [k // 94 - 1, k % 94]))   # noqa: E731
+    head = ["$date today $end", "$timescale 1ps $end", "$scope module top $end"]
+    sigs = []
+    for k in range(n_scalar):
+        head.append(f"$var wire 1 {code(k)} s{k} $end")
+        sigs.append((code(k), 0))
+    for b in range(n_bus):
+        w = int(rng.integers(2, 9))
+        c = code(n_scalar + b)
+        if b % 2:
+            head.append(f"$var wire {w} {c} v{b} [0:{w - 1}] $end")
+        else:
+            head.append(f"$var wire {w} {c} v{b} [{w - 1}:0] $end")
+        sigs.append((c, w))
+    head += ["$upscope $end", "$enddefinitions $end"]
+    body = ["#0", "$dumpvars"]
+    alpha = "01xz"
+
+    def val(w):
+        return alpha[int(rng.choice(4, p=[0.45, 0.45, 0.06, 0.04]))] if w == 0 else \
+            "".join(alpha[int(x)] for x in rng.choice(4, size=w, p=[0.45, 0.45, 0.06, 0.04]))
+
+    for c, w in sigs:
+        body.append(val(w) + c if w == 0 else f"b{val(w)} {c}")
+    body.append("$end")
+    t = 0
+    for _ in range(n_times):
+        t += int(rng.integers(1, 40))
+        body.append(f"#{t}")
+        for j in rng.permutation(len(sigs))[: int(rng.integers(1, len(sigs) + 1))]:
+            c, w = sigs[int(j)]
+            body.append(val(w) + c if w == 0 else f"b{val(w)} {c}")
+    return "\n".join(head + body) + "\n"

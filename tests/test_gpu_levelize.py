@@ -84,3 +84,17 @@ def test_gls_process_gpu_levelize_writes_the_same_file(libgls, tmp_path):
         assert r.returncode == 0, r.stdout
         outs[len(flag)] = dst.read_bytes()
     assert outs[0] == outs[1]
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_gpu_levels_match_reference_code(seed, gpu, tmp_path):
+    """gls_levelize against the reference's own TopologyOrder
+    (src/process.cpp:90-176, compiled from the reference sources)."""
+    from oracle import build
+    from test_levelize_reference import random_instances, reference_levels
+    if build.build_reference() is None or not build.REF_LEVELS_BIN.exists():
+        pytest.skip("reference sources not available on this machine")
+    ins, outs = random_instances(100 + seed, 500 + 500 * seed)
+    ref = reference_levels(build.REF_LEVELS_BIN, ins, outs, tmp_path)
+    order, level_start = levelize_gpu(*netlist_preds(ins, outs))
+    assert [order[level_start[k]:level_start[k + 1]].tolist() for k in range(len(level_start) - 1)] == ref

@@ -150,3 +150,57 @@ def test_gls_simulate_gpu_vcd_same_saif(libgls, tmp_path):
         assert r.returncode == 0, r.stdout + r.stderr
         saifs.append(out.read_text())
     assert saifs[0] == saifs[1]
+
+
+GPU_READER = r"""
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include "vcd.h"
+int main(int argc, char **argv)
+{
+    std::ifstream f(argv[1], std::ios::binary);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    glsh::VcdData v;
+    std::string err;
+    const int rc = glsh::parse_vcd_gpu(ss.str(), v, &err, 0);
+    if (rc < 0) { printf("ERR %s\n", err.c_str()); return 1; }
+    if (rc == 0) { printf("ERR the host read the body\n"); return 1; }
+    for (size_t k = 0; k < v.names.size(); ++k) {
+        printf("%s", v.names[k].c_str());
+        for (size_t j = 0; j < v.times[k].size(); ++j)
+            printf(" %llu:%u", (unsigned long long)v.times[k][j], (unsigned)v.values[k][j]);
+        printf("\n");
+    }
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_gpu_vcd_reading_matches_reference_reader(seed, gpu, tmp_path):
+    """The GPU body scan (gls_vcd_scan through the host's parse_vcd_gpu)
+    against the reference's own VCDParser (src/VCDParser.cpp, compiled from
+    the reference sources) on VCDs as simulators write them."""
+    from cases import standard_vcd
+    from gls.build import LIB_DIR, PKG, REPO
+    from oracle import build
+    from test_vcd_host import reference_lists
+    if build.build_reference() is None or not build.REF_VCD_BIN.exists():
+        pytest.skip("reference sources not available on this machine")
+    (tmp_path / "drv.cpp").write_text(GPU_READER)
+    exe = tmp_path / "drv"
+    r = subprocess.run(["g++", "-O1", "-std=c++17", f"-I{REPO / 'include'}", f"-I{PKG / 'host'}", str(tmp_path / "drv.cpp"),
+                        str(PKG / "host" / "vcd.cpp"), f"-L{LIB_DIR}", "-lgls", f"-Wl,-rpath,{LIB_DIR}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    (tmp_path / "s.vcd").write_text(standard_vcd(50 + seed, n_scalar=20, n_bus=6, n_times=3000))
+    exp = reference_lists(build.REF_VCD_BIN, tmp_path / "s.vcd", 10**9)
+    r = subprocess.run([str(exe), str(tmp_path / "s.vcd")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    got = {}
+    for line in r.stdout.splitlines():
+        parts = line.split()
+        got[parts[0]] = [tuple(int(x) for x in p.split(":")) for p in parts[1:]]
+    assert got == exp

@@ -98,3 +98,41 @@ def test_host_vcd_reader_matches_restatement(seed, reader, tmp_path):
     exp = expected_lists(body, codes, sig)
     for k in range(sig):
         assert got.get(names[k], []) == exp[k], names[k]
+
+
+@pytest.fixture(scope="module")
+def ref_vcd():
+    from oracle import build
+    if build.build_reference() is None or not build.REF_VCD_BIN.exists():
+        pytest.skip("reference sources not available on this machine")
+    return build.REF_VCD_BIN
+
+
+def reference_lists(exe, path, t_end):
+    """Every declared bit's change list as the reference's own reader gives it."""
+    r = subprocess.run([str(exe), str(path), "0", str(t_end)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    out = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("@ "):
+            parts = line[2:].split()
+            out[parts[0]] = [tuple(int(x) for x in p.split(":")) for p in parts[1:]]
+    return out
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_host_vcd_reader_matches_reference_reader(seed, reader, ref_vcd, tmp_path):
+    """The host reader against the reference's VCDParser (src/VCDParser.cpp,
+    compiled from the reference sources) on VCDs as simulators write them."""
+    from cases import standard_vcd
+    (tmp_path / "s.vcd").write_text(standard_vcd(seed, n_scalar=10 + seed, n_bus=3 + seed))
+    exp = reference_lists(ref_vcd, tmp_path / "s.vcd", 10**9)
+    r = subprocess.run([str(reader), str(tmp_path / "s.vcd")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    got = {}
+    for line in r.stdout.splitlines():
+        parts = line.split()
+        got[parts[0]] = [tuple(int(x) for x in p.split(":")) for p in parts[1:]]
+    assert set(got) == set(exp)
+    for name in exp:
+        assert got[name] == exp[name], name
