@@ -454,28 +454,50 @@ def batched_arm(args):
     all windows with gls_run_batched (waves of windows, one launch per kernel
     and level over a wave, graph replay, pools freed after each wave); the
     same windows as sequential plain runs (one gls_run each, exact
-    allocation) are timed beside it."""
+    allocation) are timed beside it.  With N ranks every rank takes its
+    share of the windows, split by predicted work (the window's length in
+    cycles: every window draws its toggle rates from the same distribution)
+    with no exchange; times are the maximum over ranks, gate-events the sum."""
     import torch
     from gls import synth
     from gls.capi import ALLOC_BOUND, ALLOC_EXACT, ALLOC_LEARNED, Simulator
     from gls.netlist import Stimulus
-    torch.cuda.set_device(0)
+    from gls.replicas import max_over_ranks, partition_windows, world_rank
+
+    world, rank, local = world_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
     cfg, nl = make_workload("c2", args.seed, args.cells, args.depth, None)
     rng = np.random.default_rng(args.seed + 4)
     n_win = args.windows or C4_WINDOWS
     lengths = rng.integers(C4_MIN_CYCLES, C4_MAX_CYCLES + 1, size=n_win)
+    mine = partition_windows(lengths, world)[rank]
     t0 = time.time()
     wins = []
-    for k, cyc in enumerate(lengths.tolist()):
-        c = synth.scaled(cfg, cycles=int(cyc))
+    for k in mine:
+        c = synth.scaled(cfg, cycles=int(lengths[k]))
         st = synth.make_stimulus(c, nl.ppi_nets, seed=args.seed + 100 + k)
         # pinned host copies: the end-to-end leg uploads from them
         p = {f: torch.from_numpy(np.ascontiguousarray(getattr(st, f))).pin_memory().numpy()
              for f in ("nets", "ev_start", "time", "value")}
         wins.append((Stimulus(p["nets"], p["ev_start"], p["time"], p["value"]), c.t_end))
-    log(f"c4: {n_win} windows, {int(lengths.sum())} cycles, "
+    my_cycles = int(lengths[mine].sum()) if mine else 0
+    log(f"c4 rank {rank}/{world}: {len(mine)} of {n_win} windows, {my_cycles} cycles, "
         f"{sum(len(w[0].time) for w in wins)} stimulus events ({time.time() - t0:.1f}s)")
     alloc = {"bound": ALLOC_BOUND, "exact": ALLOC_EXACT, "learned": ALLOC_LEARNED}[args.alloc]
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def total(x):   # summed over ranks
+        if world == 1:
+            return float(x)
+        t = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t)
+        return float(t.item())
 
     def batched_pass(sim):
         sim.clear_windows()
@@ -484,7 +506,7 @@ def batched_arm(args):
         sim.run_batched(saif_only=True)
         return [sim.saif(k) for k in range(len(wins))]
 
-    sim = Simulator(alloc_mode=alloc)
+    sim = Simulator(device=local, alloc_mode=alloc)
     if args.alloc == "learned":
         from gls import presize
         sim.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
@@ -496,8 +518,9 @@ def batched_arm(args):
     for _ in range(args.warmup):
         batched_pass(sim)
     stats = sim.stats()
-    gate_ev = stats["gate_events"]
-    with ClockSampler(0) as clk:
+    gate_ev = total(stats["gate_events"])
+    barrier()
+    with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         dev_ms = 0.0
@@ -506,15 +529,18 @@ def batched_arm(args):
             dev_ms += sim.stats()["kernel_ms"]
         torch.cuda.synchronize()
         step_s = (time.perf_counter() - t0) / args.steps
-    dev_s = dev_ms / 1000.0 / args.steps
+    barrier()
+    dev_s = max_over_ranks(dev_ms / 1000.0 / args.steps, "cuda")
+    step_s = max_over_ranks(step_s, "cuda")
     launches = sim.stats()["launches"]
     pool_b = sim.stats()["pool_bytes"]
     sim.close()
     # sequential plain runs of the same windows (exact allocation, one gls_run each)
-    plain = Simulator(alloc_mode=ALLOC_EXACT)
+    plain = Simulator(device=local, alloc_mode=ALLOC_EXACT)
     plain.load(nl)
     plain_s = 0.0
     for rep in range(2):   # the first pass warms up
+        barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for st, t_end in wins:
@@ -524,29 +550,35 @@ def batched_arm(args):
             plain.saif(w)
         torch.cuda.synchronize()
         plain_s = time.perf_counter() - t0
+    plain_s = max_over_ranks(plain_s, "cuda")
     plain.close()
+    cycles = total(my_cycles)
+    h2d = total(sum(st.time.nbytes + st.value.nbytes for st, _ in wins))
     line = {
-        "metric": "gate-events/s", "value": gate_ev / dev_s, "unit": "gate-events/s", "n_gpus": 1,
+        "metric": "gate-events/s", "value": gate_ev / dev_s, "unit": "gate-events/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": bench_config(args),
         "schedule": tune["best"],
-        "cycles": int(lengths.sum()),
+        "cycles": int(cycles),
+        "windows_per_rank": len(mine), "split": "windows over ranks by predicted work (cycles), no exchange",
         "value_timing": "device time of the waves (stimulus uploads between waves excluded); e2e: wall clock "
-                        "of add_window + run_batched + SAIF reads",
-        "sim_cycles_per_s": float(lengths.sum()) / dev_s,
+                        "of add_window + run_batched + SAIF reads; both the maximum over ranks",
+        "sim_cycles_per_s": cycles / dev_s,
         "gate_events_per_step": gate_ev,
-        "e2e": {"value": gate_ev / step_s, "unit": "gate-events/s",
-                "h2d_bytes_per_step": int(sum(st.time.nbytes + st.value.nbytes for st, _ in wins)),
+        "e2e": {"value": gate_ev / step_s, "unit": "gate-events/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(24 * nl.n_nets * n_win), "ms_per_step": 1000.0 * step_s},
         "plain_sequential": {"value": gate_ev / plain_s, "unit": "gate-events/s", "ms": 1000.0 * plain_s,
-                             "what": f"{n_win} sequential gls_run calls, exact allocation, wall clock"},
+                             "what": "the same windows as sequential gls_run calls, exact allocation, wall clock"},
         "batched_over_plain": plain_s / step_s,
         "gpu_launches": int(launches),
         "pool_bytes": pool_b,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def main():

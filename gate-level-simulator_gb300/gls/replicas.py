@@ -40,3 +40,20 @@ def max_over_ranks(x: float, device: str = "cpu") -> float:
 def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
     """Units of all ranks (each did units_per_rank) over the slowest rank's time."""
     return units_per_rank * world / seconds
+
+
+def partition_windows(work, world: int) -> list[list[int]]:
+    """Independent stimulus windows split over `world` ranks by predicted
+    work (e.g. the window's length in cycles): longest first, each to the
+    rank with the least work so far (ties to the lower rank).  Every rank
+    gets its windows in increasing index order; the split is the same on
+    every rank, so no exchange is needed to agree on it."""
+    import heapq
+    order = sorted(range(len(work)), key=lambda k: (-float(work[k]), k))
+    heap = [(0.0, r) for r in range(world)]
+    out = [[] for _ in range(world)]
+    for k in order:
+        load, r = heapq.heappop(heap)
+        out[r].append(k)
+        heapq.heappush(heap, (load + float(work[k]), r))
+    return [sorted(x) for x in out]

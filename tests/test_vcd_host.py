@@ -136,3 +136,17 @@ def test_host_vcd_reader_matches_reference_reader(seed, reader, ref_vcd, tmp_pat
     assert set(got) == set(exp)
     for name in exp:
         assert got[name] == exp[name], name
+
+
+@pytest.mark.parametrize("case", range(2))
+def test_host_vcd_reader_matches_reference_golden(case, reader, tmp_path):
+    """The host reader against the golden digests of the reference reader's
+    change lists (tests/golden/vcd_reference.json)."""
+    from cases import standard_vcd
+    from test_gpu_vcd import golden_vcd_cases, list_digests
+    c = golden_vcd_cases()[case]
+    (tmp_path / "s.vcd").write_text(standard_vcd(c["seed"], n_scalar=c["n_scalar"], n_bus=c["n_bus"],
+                                                 n_times=c["n_times"]))
+    r = subprocess.run([str(reader), str(tmp_path / "s.vcd")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert list_digests(r.stdout) == c["lists"]
