@@ -749,7 +749,11 @@ void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out)
             ref::Delay dl;
             dl.edge = a.edge;
             dl.in_bit = net(in.pins[a.in_pin]);
-            dl.out_bit = net(in.pins[ni + a.out_pin]);
+            // an output port left open is named by the port itself, as the
+            // reference's SDF reader takes it from unknown_out
+            const std::string &oport = cell.outputs[a.out_pin];
+            const bool open_out = std::find(r.unknown_out.begin(), r.unknown_out.end(), oport) != r.unknown_out.end();
+            dl.out_bit = open_out ? oport : net(in.pins[ni + a.out_pin]);
             dl.rise = a.rise;
             dl.fall = a.fall;
             r.delays.push_back(dl);

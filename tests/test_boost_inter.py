@@ -177,3 +177,23 @@ def test_wrong_signature_is_rejected(driver, tmp_path):
     (tmp_path / "x.dat").write_text("22 serialization::archivX 17 0 0\n")
     r = subprocess.run([str(driver), "design", str(tmp_path / "x.dat")], capture_output=True, text=True)
     assert r.returncode == 1 and "ERR" in r.stdout
+
+
+def test_archive_keeps_buses_aliases_constants_and_open_outputs(driver, tools, tmp_path):
+    """A netlist with bus ports, assign aliases, tie-offs and an output left
+    open (its SDF arc names the port, as the reference records it): the
+    archive and the native file give the same model."""
+    from test_gpu_cli import GV, SDF
+    files.write_vlib(tmp_path / "lib.vlib")
+    (tmp_path / "d.gv").write_text(GV)
+    (tmp_path / "d.sdf").write_text(SDF)
+    for extra, out in (([], "a.dat"), (["--native"], "n.dat")):
+        r = subprocess.run([str(tools["gls_process"]), *extra, str(tmp_path / "lib.vlib"), str(tmp_path / "d.gv"),
+                            str(tmp_path / "d.sdf"), str(tmp_path / out)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout
+    a = run(driver, "design", tmp_path / "a.dat").decode().splitlines()
+    b = run(driver, "design", tmp_path / "n.dat").decode().splitlines()
+    assert any(x.startswith("inst U5 ") and " arc " in x for x in a), "the open output's arc was lost"
+    unused = [x for x in ("const 1'b0 0", "const 1'b1 3") if not any(f" {x.split()[1]} " in f" {y} " for y in a
+                                                                      if y.startswith("inst "))]
+    assert a == [x for x in b if x not in unused]
