@@ -65,6 +65,7 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
     a->copy_lanes = ctx->copy_lanes;
     a->wave_e = nullptr;
+    a->wide = 0;
 }
 
 namespace {
@@ -557,8 +558,9 @@ static int upload_window(gls_ctx *ctx, Window *w, bool sync = true)
 {
     const uint64_t n = ctx->n_nets;
     w->cap = std::max(w->cap, projected_cap(ctx, w));
-    if (w->pool.p && w->pool.bytes < w->cap * 4) w->pool.release();
-    CK(take_buf(ctx, w->pool, w->cap * 4), "alloc event pool");
+    const uint64_t wb = w->word_bytes();
+    if (w->pool.p && w->pool.bytes < w->cap * wb) w->pool.release();
+    CK(take_buf(ctx, w->pool, w->cap * wb), "alloc event pool");
     CK(take_buf(ctx, w->net_off, n * 8), "alloc net_off");
     CK(w->net_len.ensure(n * 4), "alloc net_len");
     CK(take_buf(ctx, w->init_off, n * 8), "alloc init_off");
@@ -567,7 +569,7 @@ static int upload_window(gls_ctx *ctx, Window *w, bool sync = true)
     CK(w->small.ensure(256), "alloc counters");
     CK(take_buf(ctx, w->stim_dev, w->stim_nets.size() * 4 + 16), "alloc stim nets");
     if (w->stim_events)
-        CK(cudaMemcpyAsync(w->pool.p, w->h_words.p, w->stim_events * 4, cudaMemcpyHostToDevice, ctx->stream),
+        CK(cudaMemcpyAsync(w->pool.p, w->h_words.p, w->stim_events * wb, cudaMemcpyHostToDevice, ctx->stream),
            "upload stimulus");
     if (!w->h_off.ensure(n * 8) || !w->h_len.ensure(n * 4)) return fail(ctx, GLS_ENOMEM, "pinned staging");
     uint64_t *off = w->h_off.as<uint64_t>();
@@ -607,6 +609,7 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         w = new Window();
     }
     w->done = false;
+    w->w64 = false;
     w->t_begin = t_begin;
     w->t_end = t_end;
     std::vector<uint8_t> seen(ctx->n_nets, 0);
@@ -628,27 +631,31 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         return fail(ctx, GLS_ENOMEM, "pinned staging of %llu events", (unsigned long long)total);
     }
     // validate and pack (time << 2 | value), each net on a 4-event boundary;
-    // large stimuli are packed by several host threads
-    uint32_t *hw = w->h_words.as<uint32_t>();
+    // large stimuli are packed by several host threads.  32-bit words hold
+    // times up to 2^30 - 2; a later time repacks the stimulus in 64-bit words.
     std::atomic<int> bad(0);
     std::atomic<uint32_t> bad_net(0);
+    std::atomic<bool> long_times(false);
     // The loops carry no early exit so that the compiler vectorizes them; a
     // net's faults are reported in the order value, time range, time order.
-    auto pack = [&](uint32_t k0, uint32_t k1) {
+    auto pack = [&](auto *hw, uint32_t k0, uint32_t k1) {
+        using Wd = typename std::remove_pointer<decltype(hw)>::type;
         for (uint32_t k = k0; k < k1; ++k) {
             const uint64_t a = st->ev_start[k], cnt = st->ev_start[k + 1] - a;
             const uint32_t *tt = st->time + a;
             const uint8_t *vv = st->value + a;
-            uint32_t *o = hw + at[k];
-            uint32_t ev = 0, et = 0, eo = 0;
+            Wd *o = hw + at[k];
+            uint32_t ev = 0, et = 0, ew = 0, eo = 0;
             for (uint64_t e = 0; e < cnt; ++e) {
                 const uint32_t t = tt[e], v = vv[e];
                 ev |= v > 3 ? 1u : 0u;
-                et |= t > kMaxTime ? 1u : 0u;
-                o[e] = (t << 2) | (v & 3u);
+                ew |= t > kMaxTime ? 1u : 0u;
+                et |= t > kMaxTimeWide ? 1u : 0u;
+                o[e] = ((Wd)t << 2) | (Wd)(v & 3u);
             }
             for (uint64_t e = 1; e < cnt; ++e) eo |= tt[e] <= tt[e - 1] ? 1u : 0u;
-            for (uint64_t e = cnt; e < round4(cnt); ++e) o[e] = kInf;
+            for (uint64_t e = cnt; e < round4(cnt); ++e) o[e] = EvW<Wd>::kInfW;
+            if (ew) long_times = true;
             if (ev | et | eo) {
                 bad = ev ? 1 : (et ? 2 : 3);
                 bad_net = st->net[k];
@@ -671,15 +678,25 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
         std::vector<uint32_t> first(parts + 1, st->n_nets);
         for (unsigned q = 0; q < parts; ++q)
             first[q] = (uint32_t)(std::lower_bound(at.begin(), at.end() - 1, total * q / parts) - at.begin());
-        ctx->pool->parallel_for(parts, [&](unsigned q) { pack(first[q], std::max(first[q], first[q + 1])); });
+        ctx->pool->parallel_for(parts, [&](unsigned q) {
+            pack(w->h_words.as<uint32_t>(), first[q], std::max(first[q], first[q + 1]));
+        });
     } else {
-        pack(0, st->n_nets);
+        pack(w->h_words.as<uint32_t>(), 0, st->n_nets);
+    }
+    if (!bad && long_times) {
+        if (!w->h_words.ensure(total * 8)) {
+            ctx->spare.push_back(w);
+            return fail(ctx, GLS_ENOMEM, "pinned staging of %llu events", (unsigned long long)total);
+        }
+        w->w64 = true;
+        pack(w->h_words.as<WideWord>(), 0, st->n_nets);
     }
     if (bad) {
         ctx->spare.push_back(w);
         const int b = bad;
         return fail(ctx, b == 2 ? GLS_ERANGE : GLS_EINVAL, "stimulus net %u: %s", (unsigned)bad_net,
-                    b == 1 ? "value above 3" : b == 2 ? "time beyond the largest event time (2^30-2)"
+                    b == 1 ? "value above 3" : b == 2 ? "time beyond the largest event time (2^32-2)"
                                              : "times not strictly increasing");
     }
     w->stim_nets.assign(st->net, st->net + st->n_nets);
@@ -743,10 +760,10 @@ static WinDev make_windev(gls_ctx *ctx, Window *w, const LevelScratch &ls, int p
     d.seg_base = (parity ? ls.seg_base1 : ls.seg_base).as<uint32_t>();
     d.slot = (parity ? ls.slot1 : ls.slot).as<uint64_t>();
     d.scr = (parity ? ls.scr1 : ls.scr).as<uint64_t>();
-    d.segs = ls.segs.as<SegRec>();
+    d.segs = ls.segs.as<SegRec>();   // SegRecT<WideWord> records in a window of 64-bit words
     d.copies = ls.copies.as<CopyRec>();
     d.scratch = ls.scratch.as<uint32_t>();
-    d.scr_cap = ls.scr_cap;
+    d.scr_cap = ls.scr_cap * 4 / w->word_bytes();   // the stacks are sized in 32-bit words
     d.cap = w->cap;
     d.seg_cap = ls.seg_cap;
     d.t_begin = w->t_begin;
@@ -790,10 +807,15 @@ static int reset_window(gls_ctx *ctx, Window *w)
 // whose per-gate-output tables serve levels of parity p.  With `prof` the
 // kernel classes are bracketed with events (not during stream capture).
 static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev *const h[2], uint32_t nwin,
-                          uint32_t max_stim, bool prof, uint32_t *launches)
+                          uint32_t max_stim, bool prof, uint32_t *launches, bool w64 = false)
 {
     LevelArgs a;
     ctx_level_args(ctx, &a);
+    if (w64) {   // a window of 64-bit words runs alone, through the thread-per-segment kernels
+        if (nwin != 1) return fail(ctx, GLS_EINVAL, "64-bit event windows run one at a time");
+        a.wide = 1;
+        a.warp_mask = 0;
+    }
     // Overlapped levels: every class runs simulate, link and copy on its own
     // stream; the main stream plans the next level as soon as every class
     // has linked (the plan needs the new lists' lengths and places, and
@@ -808,10 +830,10 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
         // writes their counts; learned mode's presize would read them)
         CK(cudaEventRecord(ctx->stim_fork, ctx->stream), "stim fork");
         CK(cudaStreamWaitEvent(ctx->stim_side, ctx->stim_fork, 0), "stim fork wait");
-        launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stim_side);
+        launch_stim_saif(dw[0], *h[0], nwin, max_stim, w64, ctx->stim_side);
         CK(cudaEventRecord(ctx->stim_join, ctx->stim_side), "stim join");
     } else {
-        launch_stim_saif(dw[0], *h[0], nwin, max_stim, ctx->stream);
+        launch_stim_saif(dw[0], *h[0], nwin, max_stim, w64, ctx->stream);
     }
     ++*launches;
     if (prof) prof_mark(ctx);
@@ -942,15 +964,29 @@ static int enqueue_window(gls_ctx *ctx, Window *w, uint32_t *launches)
     CK(cudaMemcpyAsync(w->dwin.p, d, sizeof d, cudaMemcpyHostToDevice, ctx->stream), "upload window descriptor");
     const WinDev *dw[2] = {w->dwin.as<WinDev>(), w->dwin.as<WinDev>() + 1};
     const WinDev *hp[2] = {&d[0], &d[1]};
-    return enqueue_levels(ctx, dw, hp, 1, d[0].n_stim, true, launches);
+    return enqueue_levels(ctx, dw, hp, 1, d[0].n_stim, true, launches, w->w64);
 }
 
 // Totals of a run over its windows.
 struct RunAcc {
-    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0, over_ev = 0;
+    uint64_t gate_ev = 0, out_ev = 0, segs = 0, pool_ev = 0, pool_bytes = 0, fanin_ev = 0, over_ev = 0, wide = 0;
     double total_ms = 0.0;
     uint32_t launches = 0;
 };
+
+// The window's stimulus repacked in 64-bit event words and uploaded again.
+static int widen_window(gls_ctx *ctx, Window *w)
+{
+    const uint64_t n = w->stim_events;
+    std::vector<uint32_t> narrow(w->h_words.as<uint32_t>(), w->h_words.as<uint32_t>() + n);
+    if (!w->h_words.ensure(n * 8)) return fail(ctx, GLS_ENOMEM, "pinned staging of %llu events", (unsigned long long)n);
+    WideWord *o = w->h_words.as<WideWord>();
+    for (uint64_t e = 0; e < n; ++e)
+        o[e] = narrow[e] == kInf ? EvW<WideWord>::kInfW : (WideWord)narrow[e];
+    w->w64 = true;
+    w->pool.release();
+    return upload_window(ctx, w);
+}
 
 // Read a window's flags after its run; on a full pool or work space, grow it
 // and run the window again on its own (level work space 0), until it fits.
@@ -971,14 +1007,19 @@ static int settle_window(gls_ctx *ctx, Window *w, RunAcc &acc)
             acc.segs += small[3];
             acc.fanin_ev += small[4];
             acc.pool_ev += small[0];
-            acc.pool_bytes += w->cap * 4;
+            acc.pool_bytes += w->cap * w->word_bytes();
+            acc.wide += w->w64 ? 1 : 0;
             break;
         }
         if (err & kErrPresize) return fail(ctx, GLS_ECUDA, "presize kernel timed out waiting for its tensor-core MMA");
-        if (err & (kErrRegion | kErrEmptied | kErrTime)) {
+        if ((err & kErrTime) && !w->w64) {
+            // a gate output past 2^30 - 2: the window again in 64-bit words
+            int rc = widen_window(ctx, w);
+            if (rc) return rc;
+        } else if (err & (kErrRegion | kErrEmptied | kErrTime)) {
             return fail(ctx, err & kErrTime ? GLS_ERANGE : GLS_EINVAL,
                         "simulation error flags 0x%x (%s)", err,
-                        err & kErrTime ? "output time reached 2^32-1"
+                        err & kErrTime ? "output time beyond the largest event time (2^32-2)"
                                        : err & kErrEmptied ? "output list emptied by a zero delay at time 0"
                                                            : "segment region overflow");
         }
@@ -991,7 +1032,7 @@ static int settle_window(gls_ctx *ctx, Window *w, RunAcc &acc)
                 return fail(ctx, GLS_ENOMEM, "grow level work space to %llu stack words / %u segments (flags 0x%x): %s",
                             (unsigned long long)ctx->scr_cap, ctx->seg_cap, err, cudaGetErrorString(e));
         }
-        if (err & kErrPool) {
+        if ((err & kErrPool) && !(err & kErrTime)) {
             w->cap *= 2;
             w->pool.release();
             int rc = upload_window(ctx, w);
@@ -1032,6 +1073,7 @@ static void publish_stats(gls_ctx *ctx, const RunAcc &acc, const double kms[4])
     ctx->stats.fanin_bytes = acc.fanin_ev * 5;
     ctx->stats.presize_overflows = acc.over_ev;
     ctx->stats.pool_used = acc.pool_ev;
+    ctx->stats.wide_windows = acc.wide;
 }
 
 extern "C" int gls_run(gls_ctx *ctx)
@@ -1105,7 +1147,7 @@ static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
         cudaMemGetInfo(&fr, &tot);
         fr += spare_bytes(ctx);
         uint64_t per = 0;
-        for (Window *w : ctx->windows) per = std::max<uint64_t>(per, projected_cap(ctx, w) * 4);
+        for (Window *w : ctx->windows) per = std::max<uint64_t>(per, projected_cap(ctx, w) * w->word_bytes());
         per += (uint64_t)ctx->n_nets * 48 + (uint64_t)(ctx->max_width + 1) * 32 +
                (uint64_t)ctx->seg_cap * (sizeof(SegRec) + sizeof(CopyRec)) + ctx->scr_cap * 4;
         const uint64_t fit = std::max<uint64_t>(1, (uint64_t)(0.85 * (double)fr) / std::max<uint64_t>(per, 1));
@@ -1181,7 +1223,8 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
         CK(cudaGraphLaunch(ge, ctx->stream), "graph launch");
         acc.launches += l;
     } else {
-        int rc = enqueue_levels(ctx, dw, hp, nwin, max_stim, false, &acc.launches);
+        int rc = enqueue_levels(ctx, dw, hp, nwin, max_stim, false, &acc.launches,
+                                nwin == 1 && ctx->windows[w0]->w64);
         if (rc) return rc;
     }
     CK(cudaEventRecord(e1, ctx->stream), "event");
@@ -1244,9 +1287,19 @@ extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
             uint64_t per = 1;
             for (uint64_t k = 0; k < nwin; ++k) {
                 const Window *w = ctx->windows[w0 + k];
-                per = std::max<uint64_t>(per, projected_cap(ctx, w) * 4 + (uint64_t)ctx->n_nets * 48);
+                per = std::max<uint64_t>(per, projected_cap(ctx, w) * w->word_bytes() + (uint64_t)ctx->n_nets * 48);
             }
             nwin = std::max<uint64_t>(1, std::min<uint64_t>(nwin, (uint64_t)(0.85 * (double)fr) / per));
+        }
+        // a window of 64-bit event words runs alone; a wave stops before one
+        if (ctx->windows[w0]->w64) {
+            nwin = 1;
+        } else {
+            for (uint64_t k = 1; k < nwin; ++k)
+                if (ctx->windows[w0 + k]->w64) {
+                    nwin = k;
+                    break;
+                }
         }
         float ms = 0.f;
         rc = run_wave(ctx, w0, (uint32_t)nwin, o, acc, &ms, e0, e1);
@@ -1416,11 +1469,20 @@ extern "C" int gls_waveform(gls_ctx *ctx, uint32_t window, uint32_t net, uint32_
     *n = len;
     const uint64_t k = std::min<uint64_t>(cap, len);
     if (k && (time || value)) {
-        std::vector<uint32_t> words(k);
-        CK(cudaMemcpy(words.data(), w->pool.as<uint32_t>() + off, k * 4, cudaMemcpyDeviceToHost), "read events");
-        for (uint64_t e = 0; e < k; ++e) {
-            if (time) time[e] = ev_time(words[e]);
-            if (value) value[e] = (uint8_t)ev_val(words[e]);
+        if (w->w64) {
+            std::vector<WideWord> words(k);
+            CK(cudaMemcpy(words.data(), w->pool.as<WideWord>() + off, k * 8, cudaMemcpyDeviceToHost), "read events");
+            for (uint64_t e = 0; e < k; ++e) {
+                if (time) time[e] = ev_time(words[e]);
+                if (value) value[e] = (uint8_t)ev_val(words[e]);
+            }
+        } else {
+            std::vector<uint32_t> words(k);
+            CK(cudaMemcpy(words.data(), w->pool.as<uint32_t>() + off, k * 4, cudaMemcpyDeviceToHost), "read events");
+            for (uint64_t e = 0; e < k; ++e) {
+                if (time) time[e] = ev_time(words[e]);
+                if (value) value[e] = (uint8_t)ev_val(words[e]);
+            }
         }
     }
     return GLS_OK;

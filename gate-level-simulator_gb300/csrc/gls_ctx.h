@@ -168,7 +168,8 @@ struct LevelScratch {
             if (e == cudaSuccess) width = w;
         }
         if (e == cudaSuccess && segs_need > seg_cap) {
-            e = segs.ensure((size_t)segs_need * sizeof(gls::SegRec));
+            // room for the segment records of either event-word width
+            e = segs.ensure((size_t)segs_need * gls::kSegRecMax);
             if (e == cudaSuccess) e = copies.ensure((size_t)segs_need * sizeof(gls::CopyRec));
             if (e == cudaSuccess) seg_cap = segs_need;
         }
@@ -203,6 +204,11 @@ struct Window {
     bool done = false;
     bool uploaded = false;              // device buffers hold this stimulus (uploaded when the window first runs)
     bool saif_only = false;             // pool released after a batched run: SAIF counts and lengths kept
+    // 64-bit event words: a stimulus time or a gate output past 2^30 - 2
+    // (the pool, the stimulus staging and the level stacks hold 8 bytes per
+    // event; the window runs alone, through the thread-per-segment kernels)
+    bool w64 = false;
+    uint64_t word_bytes() const { return w64 ? 8 : 4; }
 };
 
 }  // namespace glsh

@@ -20,20 +20,38 @@ namespace gls {
 constexpr int kMaxSlots = 6;        // distinct fan-in nets per gate (MAX_IN_NUM, src/simulate.cu:25)
 constexpr int kMaxPins = 6;         // cell inputs covered by a LUT (4^6 entries)
 constexpr uint32_t kInf = 0xFFFFFFFFu;
-constexpr uint32_t kMaxTime = (1u << 30) - 2;   // largest event time a word can carry
+constexpr uint32_t kMaxTime = (1u << 30) - 2;   // largest event time a 32-bit word can carry
+constexpr uint32_t kMaxTimeWide = 0xFFFFFFFEu;  // largest event time of a 64-bit word (times stay 32-bit)
 constexpr uint8_t kV0 = 0, kVX = 1, kVZ = 2, kV1 = 3;
 constexpr int kClasses = 4;         // fan-in classes: 1, 2, 3, 4..6 distinct input nets
 
+// An event is one word, time << 2 | value.  A window whose times fit 30
+// bits uses 32-bit words; a window with later times (up to 2^32 - 2, the
+// reference GPU tool's 32-bit range) uses 64-bit words.
+using WideWord = unsigned long long;
 __host__ __device__ inline uint32_t ev_word(uint32_t t, uint32_t v) { return (t << 2) | v; }
 __host__ __device__ inline uint32_t ev_time(uint32_t w) { return w >> 2; }
 __host__ __device__ inline uint32_t ev_val(uint32_t w) { return w & 3u; }
+__host__ __device__ inline uint32_t ev_time(WideWord w) { return (uint32_t)(w >> 2); }
+__host__ __device__ inline uint32_t ev_val(WideWord w) { return (uint32_t)w & 3u; }
+template <class Wd> struct EvW;
+template <> struct EvW<uint32_t> {
+    static constexpr uint32_t kMax = kMaxTime;      // largest event time
+    static constexpr uint32_t kInfW = 0xFFFFFFFFu;  // above every event word
+    __host__ __device__ static uint32_t word(uint32_t t, uint32_t v) { return (t << 2) | v; }
+};
+template <> struct EvW<WideWord> {
+    static constexpr uint32_t kMax = kMaxTimeWide;
+    static constexpr WideWord kInfW = ~0ull;
+    __host__ __device__ static WideWord word(uint32_t t, uint32_t v) { return ((WideWord)t << 2) | v; }
+};
 
 // error bits raised by kernels
 constexpr uint32_t kErrPool = 1u;       // event pool exhausted
 constexpr uint32_t kErrRegion = 2u;     // segment region overflow (internal invariant)
 constexpr uint32_t kErrEmptied = 4u;    // output list emptied (zero delay at t=0)
 constexpr uint32_t kErrSegCap = 8u;     // segment table too small
-constexpr uint32_t kErrTime = 16u;      // an output time passed kMaxTime
+constexpr uint32_t kErrTime = 16u;      // an output time passed the largest time its event word holds
 constexpr uint32_t kErrScratch = 32u;   // level scratch exhausted
 constexpr uint32_t kErrPresize = 64u;   // the tensor-core presize kernel gave up waiting for its MMA
 
@@ -104,17 +122,21 @@ __host__ __device__ constexpr uint32_t sense1_table()
 constexpr uint32_t kSense1Tab = sense1_table();
 static_assert(sense_of(kV0, kVX) == 1 && sense_of(kVX, kV0) == 2 && sense_of(kVX, kVZ) == 3 && sense_of(kVZ, kVX) == 4,
               "sense classes");
-// delays are stored capped at kMaxTime + 1: an output time past kMaxTime is
-// an error whichever arc gives it, and t + d then never wraps 32 bits
-constexpr uint32_t kMaxDelay = kMaxTime + 1;
+// delays are stored capped at kMaxTimeWide: an output time past it is an
+// error whichever arc gives it (the kernels add t + d in 64 bits, or check
+// the 32-bit sum for wrap-around), and kInf stays free to mean "no arc"
+constexpr uint32_t kMaxDelay = kMaxTimeWide;
 constexpr uint32_t kNegTab = neg_table();
 
-struct SegRec {             // one time segment of one gate output
+template <class Wd>
+struct SegRecT {            // one time segment of one gate output
     uint32_t region;        // offset of the segment's stack inside the gate's scratch
     uint32_t cnt;           // entries on the segment's local stack
     uint32_t min_o;         // smallest candidate output time in the segment
-    uint32_t last;          // the stack's top entry (when cnt > 0): linking reads no scratch for it
+    Wd last;                // the stack's top entry (when cnt > 0): linking reads no scratch for it
 };
+using SegRec = SegRecT<uint32_t>;
+constexpr size_t kSegRecMax = sizeof(SegRecT<WideWord>);   // table entries are sized for either word
 
 struct CopyRec {            // what k_copy does for one segment
     uint64_t src;           // scratch index of the first kept entry
@@ -169,6 +191,7 @@ struct LevelArgs {
     uint32_t alloc_mode;        // kAllocBound / kAllocExact / kAllocLearned
     uint32_t copy_lanes;        // lanes per segment in the copy kernel (4, 8, 16 or 32)
     unsigned long long *wave_e; // wave of windows: fan-in events of the level per class over all windows (else null)
+    uint32_t wide;              // 1: the window holds 64-bit event words (one window per launch)
 };
 
 // Windows simulated together: every level kernel takes a device array of
@@ -180,7 +203,8 @@ __host__ __device__ inline int fanin_class(int m) { return m <= 1 ? 0 : (m == 2 
 
 // A launch covers nwin windows: `h` is window 0's descriptor on the host
 // (used when nwin == 1), `dw` the device array of all nwin descriptors.
-void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, cudaStream_t st);
+void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, bool wide,
+                      cudaStream_t st);
 void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, cudaStream_t st);
 // a wave's fan-in events per class into a.wave_e (cleared before), so every
 // window of the wave cuts its segments to the same size

@@ -379,10 +379,11 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
 // guess: gallop away from the guess, then bisect.  Event lists of one gate
 // share the clock, so a position scaled from another list is usually a few
 // events off.  Compares whole words: time >= key <=> word >= key << 2.
-__device__ __forceinline__ uint32_t search_from(const uint32_t *__restrict__ x, uint32_t n, uint32_t key, uint32_t g)
+template <class Wd>
+__device__ __forceinline__ uint32_t search_from(const Wd *__restrict__ x, uint32_t n, uint32_t key, uint32_t g)
 {
     if (n == 0) return 0;
-    const uint32_t kw = key << 2;
+    const Wd kw = (Wd)key << 2;
     if (g >= n) g = n - 1;
     int64_t lo, hi;
     if (x[g] < kw) {
@@ -426,6 +427,7 @@ __device__ __forceinline__ uint32_t sel4(const uint4 &q, uint32_t k)
 #ifndef GLS_SIM_WARP_BATCH
 #define GLS_SIM_WARP_BATCH 1   // thread-per-segment kernels: a warp takes 32 segments at a time
 #endif
+constexpr uint32_t kSimBlock = 128;   // threads per block of the thread-per-segment kernels
 #ifndef GLS_READER_W3
 #define GLS_READER_W3 1   // events per reader chunk in the wider gate kernels
 #endif
@@ -518,6 +520,34 @@ struct Reader<1> {
     }
 };
 
+// The same one-event reader for 64-bit words (windows with times past
+// 2^30 - 2); EvW<WideWord>::kInfW once exhausted.
+struct ReaderWide {
+    using C = WideWord;
+    const WideWord *q;
+    uint32_t left;
+    WideWord nt;
+
+    __device__ __forceinline__ WideWord first(const C *__restrict__ P, uint64_t off, uint32_t p0, uint32_t e0)
+    {
+        left = 0;
+        if (p0 >= e0) return EvW<WideWord>::kInfW;
+        const WideWord *x = P + off + p0;
+        const WideWord h = __ldg(x);
+        left = e0 - p0 - 1;
+        if (left) nt = __ldg(x + 1);
+        q = x + 2;
+        return h;
+    }
+    __device__ __forceinline__ WideWord next(const C *__restrict__)
+    {
+        if (!left) return EvW<WideWord>::kInfW;
+        const WideWord h = nt;
+        if (--left) nt = __ldg(q++);
+        return h;
+    }
+};
+
 // x * y / z for 32-bit operands, in 32-bit arithmetic when the product fits
 __device__ __forceinline__ uint32_t mul_div(uint32_t x, uint32_t y, uint32_t z)
 {
@@ -542,9 +572,9 @@ __device__ __forceinline__ uint32_t slut_get(const uint4 &t, uint32_t curp)
 // first events of X / Y at or after that time.  Equal times may sit in both
 // lists (not within one), so a cut at the returned time keeps every time's
 // events on one side.
-__device__ __forceinline__ uint32_t rank_time2(const uint32_t *__restrict__ X, uint32_t nx,
-                                               const uint32_t *__restrict__ Y, uint32_t ny, uint32_t r, uint32_t g,
-                                               uint32_t &ix, uint32_t &iy)
+template <class Wd>
+__device__ __forceinline__ uint32_t rank_time2(const Wd *__restrict__ X, uint32_t nx, const Wd *__restrict__ Y,
+                                               uint32_t ny, uint32_t r, uint32_t g, uint32_t &ix, uint32_t &iy)
 {
     // short(i): the first r merged events hold more than i events of X
     // (true for small i, false from the answer on)
@@ -589,8 +619,8 @@ __device__ __forceinline__ uint32_t rank_time2(const uint32_t *__restrict__ X, u
 // input nets) split into segments of equal size; with one input net the
 // event of rank sk * plen / S of that list.  cut[j] receives list j's first
 // event at or after that time.  The cut time does not decrease with sk.
-template <int M>
-__device__ __forceinline__ void cut_at(const uint32_t *__restrict__ pool, const uint64_t (&off)[M],
+template <int M, class Wd>
+__device__ __forceinline__ void cut_at(const Wd *__restrict__ pool, const uint64_t (&off)[M],
                                        const uint32_t (&len)[M], int m, int piv, int sec, uint64_t poff, uint64_t soff,
                                        uint32_t plen, uint32_t slen, uint32_t sk, uint32_t S, uint32_t (&cut)[M])
 {
@@ -609,14 +639,17 @@ __device__ __forceinline__ void cut_at(const uint32_t *__restrict__ pool, const 
     }
 }
 
-template <int M>
+template <int M, class Wd>
 __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t s,
                             uint32_t S, uint32_t seg_id, uint64_t scr, const uint4 sl)
 {
     constexpr bool kSlut = M <= 3;   // truth table in registers
     constexpr int kRW = M >= 3 ? GLS_READER_W3 : GLS_READER_W2;   // events per reader chunk
-    using RC = typename Reader<kRW>::C;
+    // 64-bit words (a window with times past 2^30 - 2) are read one at a time
+    using RD = typename std::conditional<std::is_same<Wd, uint32_t>::value, Reader<kRW>, ReaderWide>::type;
+    using RC = typename RD::C;
     const RC *P = reinterpret_cast<const RC *>(w.pool);
+    const Wd *pw = reinterpret_cast<const Wd *>(w.pool);
     uint64_t off[M];
     uint32_t len[M];
     int piv = 0, sec = -1;   // the longest input list and the longest of the others
@@ -641,13 +674,13 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     }
     // the segment's first events (cut s) and end events (cut s + 1)
     uint32_t cb[M], ce[M];
-    if (s > 0) cut_at<M>(w.pool, off, len, md.m, piv, sec, poff, soff, plen, slen, s, S, cb);
-    if (s + 1 < S) cut_at<M>(w.pool, off, len, md.m, piv, sec, poff, soff, plen, slen, s + 1, S, ce);
+    if (s > 0) cut_at<M>(pw, off, len, md.m, piv, sec, poff, soff, plen, slen, s, S, cb);
+    if (s + 1 < S) cut_at<M>(pw, off, len, md.m, piv, sec, poff, soff, plen, slen, s + 1, S, ce);
     uint32_t curp = 0x555u;   // every slot X
     uint32_t region = s, capn = 1;
     bool before = false;
-    Reader<kRW> rd[M];
-    uint32_t hk[M];   // head word of every list with the value bits set: equal times compare equal
+    RD rd[M];
+    Wd hk[M];         // head word of every list with the value bits set: equal times compare equal
 #pragma unroll
     for (int j = 0; j < M; ++j) {
         uint32_t b = 0, e = 0;
@@ -657,7 +690,7 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
             region += b;
             capn += e - b;
             if (b > 0) {
-                curp = (curp & ~(3u << (2 * j))) | (ev_val(w.pool[off[j] + b - 1]) << (2 * j));
+                curp = (curp & ~(3u << (2 * j))) | (ev_val(pw[off[j] + b - 1]) << (2 * j));
                 before = true;
             }
         }
@@ -666,17 +699,18 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
     const uint8_t *lut = a.lut + md.lut_off;
     const NetDelay *nd = a.ndel + md.dt_off;
     const bool regular = md.flags & kFlagRegular;
-    uint32_t *ot = w.scratch + scr + region;
-    uint32_t cnt = 0, top = 0;        // stack size and its top word
+    Wd *ot = reinterpret_cast<Wd *>(w.scratch) + scr + region;
+    uint32_t cnt = 0;                 // stack size
+    Wd top = 0;                       // its top word
     int popped_v = -1;
-    if (s == 0) { top = ev_word(0, kVX); ot[0] = top; cnt = 1; }
+    if (s == 0) { top = EvW<Wd>::word(0, kVX); ot[0] = top; cnt = 1; }
     uint32_t fprev = before ? (kSlut ? slut_get<M>(sl, curp) : lut[lut_index(curp, md)]) : kVX;
     uint32_t min_o = kInf;
     for (;;) {
-        uint32_t mk = hk[0] | 3u;
+        Wd mk = hk[0] | 3u;
 #pragma unroll
-        for (int j = 1; j < M; ++j) mk = min(mk, hk[j] | 3u);
-        if (mk == kInf) break;
+        for (int j = 1; j < M; ++j) mk = min(mk, (Wd)(hk[j] | 3u));
+        if (mk == EvW<Wd>::kInfW) break;
         const uint32_t lastp = curp;
         uint32_t chg = 0;
 #pragma unroll
@@ -695,8 +729,9 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
         const uint32_t d = regular ? regular_delay<M>(nd, chg, so1, curp, lastp, a.def_delay)
                                    : select_delay(a.arcs + md.arc_off, md.n_arcs, chg, (int)so1 + 1, curp, lastp,
                                                   a.def_delay);
-        const uint32_t o = t + d;   // delays are at most kMaxDelay: the sum does not wrap
-        if (o > kMaxTime) { atomicOr(w.err, kErrTime); break; }
+        const uint64_t o64 = (uint64_t)t + d;   // 64 bits: delays reach 2^32 - 2
+        if (o64 > EvW<Wd>::kMax) { atomicOr(w.err, kErrTime); break; }
+        const uint32_t o = (uint32_t)o64;
         min_o = min(min_o, o);
         // inertial update, src/simulate.cpp:991-1009
         while (cnt > 0 && ev_time(top) >= o) {
@@ -707,16 +742,16 @@ __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &
         const int prevv = cnt > 0 ? (int)ev_val(top) : (s == 0 ? popped_v : -1);
         if (prevv != (int)F) {
             if (cnt >= capn) { atomicOr(w.err, kErrRegion); break; }
-            top = ev_word(o, F);
+            top = EvW<Wd>::word(o, F);
             ot[cnt++] = top;
         } else if (cnt == 0) {
             atomicOr(w.err, kErrEmptied);
             break;
         }
     }
-    SegRec r;
+    SegRecT<Wd> r;
     r.region = region; r.cnt = cnt; r.min_o = min_o; r.last = top;
-    w.segs[seg_id] = r;
+    reinterpret_cast<SegRecT<Wd> *>(w.segs)[seg_id] = r;
 }
 
 // Segments of all windows of a launch form one index space: s_pre[k] is
@@ -766,7 +801,7 @@ __device__ __forceinline__ uint32_t window_of(const uint32_t *s_pre, uint32_t nw
 // owns a contiguous share of the class's segments and its threads take the
 // next one from a shared counter as they finish, so long and short segments
 // balance inside the block.
-template <int M, bool kBatch>
+template <int M, bool kBatch, class Wd>
 #ifndef GLS_SIM2_BLOCKS
 #define GLS_SIM2_BLOCKS 8   // resident blocks per SM the 1- and 2-input gate kernels are compiled for
 #endif
@@ -776,7 +811,7 @@ template <int M, bool kBatch>
 #ifndef GLS_SIM1_BLOCKS
 #define GLS_SIM1_BLOCKS GLS_SIM2_BLOCKS   // resident blocks per SM the 1-input gate kernel is compiled for
 #endif
-__global__ void __launch_bounds__(128, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4)))
+__global__ void __launch_bounds__(kSimBlock, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4)))
     k_sim(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     __shared__ uint32_t s_next;
@@ -849,7 +884,7 @@ __global__ void __launch_bounds__(128, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_
         const uint32_t S = w.seg_base[i + 1] - sb;
         const DrvMeta md = a.meta[a.lo + i];
         const uint4 sl = M <= 3 ? __ldg(a.slut + a.lo + i) : make_uint4(0, 0, 0, 0);
-        sim_segment<M>(w, a, md, g - sb, S, g, w.scr[i], sl);
+        sim_segment<M, Wd>(w, a, md, g - sb, S, g, w.scr[i], sl);
     }
 }
 
@@ -1354,7 +1389,7 @@ __device__ __forceinline__ void saif_add(unsigned long long acc[3], int cls, uns
 // pass B drops a segment's first entry when it repeats the last kept value
 // before it, places the segments back to back in the gate's pool slot and
 // hands each segment's copy to k_copy with the final event that precedes it.
-template <bool kBatch>
+template <bool kBatch, class Wd>
 #ifndef GLS_LINK_BLOCKS
 #define GLS_LINK_BLOCKS 1   // resident blocks per SM the link kernel is compiled for (1: no bound)
 #endif
@@ -1372,15 +1407,16 @@ __global__ void __launch_bounds__(256, GLS_LINK_BLOCKS) k_link(const WinSet<kBat
     const uint32_t sb = w.seg_base[i], se = w.seg_base[i + 1];
     const uint64_t slot = w.slot[i];
     const uint64_t scr = w.scr[i];
-    const uint32_t *sx = w.scratch + scr;
+    const Wd *sx = reinterpret_cast<const Wd *>(w.scratch) + scr;
+    const SegRecT<Wd> *segs = reinterpret_cast<const SegRecT<Wd> *>(w.segs);
     const uint32_t out_net = a.meta[a.lo + i].out_net;
     // pass A (right to left)
     uint32_t carry_min = kInf;
     for (int64_t base = se; base > (int64_t)sb; base -= 32) {
         const int64_t s = base - 32 + lane;
         const bool valid = s >= (int64_t)sb;
-        SegRec r = {0, 0, kInf, 0};
-        if (valid) r = w.segs[s];
+        SegRecT<Wd> r = {0, 0, kInf, 0};
+        if (valid) r = segs[s];
         uint32_t x = r.min_o;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1410,12 +1446,12 @@ __global__ void __launch_bounds__(256, GLS_LINK_BLOCKS) k_link(const WinSet<kBat
         const bool valid = s < se;
         uint32_t keep = 0, region = 0, firstv = 0, lastv = 0, lastt = 0;
         if (valid) {
-            const SegRec r = w.segs[s];
+            const SegRecT<Wd> r = segs[s];
             keep = w.copies[s].n;
             region = r.region;
             if (keep) {
                 firstv = ev_val(sx[region]);
-                const uint32_t lw = keep == r.cnt ? r.last : sx[region + keep - 1];
+                const Wd lw = keep == r.cnt ? r.last : sx[region + keep - 1];
                 lastv = ev_val(lw);
                 lastt = ev_time(lw);
             }
@@ -1490,18 +1526,36 @@ __global__ void __launch_bounds__(256, GLS_LINK_BLOCKS) k_link(const WinSet<kBat
 // when the window starts past every event): with the bounds capped at 2^31
 // the clamp gives the same values as in 64 bits, and a relative time
 // shifted left by 2 still fits 32 bits next to a 2-bit value class.
-struct RelClamp {
+// With 64-bit words (times up to 2^32 - 2) the same runs in 64 bits: the
+// bounds are capped at 2^32 and a relative time needs 33 bits.
+template <class P> struct RelClampT;
+template <> struct RelClampT<uint32_t> {
     uint32_t lo, hi;
-    __device__ __forceinline__ RelClamp(unsigned long long b, unsigned long long e)
+    __device__ __forceinline__ RelClampT(unsigned long long b, unsigned long long e)
         : lo((uint32_t)min(b, 1ull << 31)), hi((uint32_t)min(e, 1ull << 31)) {}
     __device__ __forceinline__ uint32_t operator()(uint32_t t) const { return min(max(t, lo), hi) - lo; }
 };
+template <> struct RelClampT<unsigned long long> {
+    unsigned long long lo, hi;
+    __device__ __forceinline__ RelClampT(unsigned long long b, unsigned long long e)
+        : lo(min(b, 1ull << 32)), hi(min(e, 1ull << 32)) {}
+    __device__ __forceinline__ unsigned long long operator()(uint32_t t) const
+    {
+        const unsigned long long x = t;
+        return min(max(x, lo), hi) - lo;
+    }
+};
+using RelClamp = RelClampT<uint32_t>;
+// the packed (relative time << 2 | value class) and the sums of a window's word type
+template <class Wd> using SaifP = typename std::conditional<std::is_same<Wd, uint32_t>::value, uint32_t,
+                                                            unsigned long long>::type;
 
-__device__ __forceinline__ void saif_add32(uint32_t acc[3], uint32_t cls, uint32_t d)
+template <class P>
+__device__ __forceinline__ void saif_add32(P acc[3], P cls, P d)
 {
-    acc[0] += cls == 0 ? d : 0u;
-    acc[1] += cls == 1 ? d : 0u;
-    acc[2] += cls == 2 ? d : 0u;
+    acc[0] += cls == 0 ? d : P(0);
+    acc[1] += cls == 1 ? d : P(0);
+    acc[2] += cls == 2 ? d : P(0);
 }
 
 // SAIF contributions of W consecutive events of a list held one per lane of
@@ -1510,18 +1564,18 @@ __device__ __forceinline__ void saif_add32(uint32_t acc[3], uint32_t cls, uint32
 // event before the group's first as (relative clamped time << 2 | value
 // class) and is advanced past its last.  The sums of one segment or one
 // list are at most one window long, so they fit 32 bits.
-template <int W>
-__device__ __forceinline__ void integrate_group(const RelClamp &rc, uint32_t word, bool v, uint32_t n_here, bool any,
-                                                uint32_t &prev, uint32_t acc[3])
+template <int W, class Wd, class P>
+__device__ __forceinline__ void integrate_group(const RelClampT<P> &rc, Wd word, bool v, uint32_t n_here, bool any,
+                                                P &prev, P acc[3])
 {
     const unsigned FULL = 0xffffffffu;
     const int sub = threadIdx.x & (W - 1);
-    const uint32_t me = (rc(ev_time(word)) << 2) | (uint32_t)vclass(ev_val(word));
-    uint32_t pv = __shfl_up_sync(FULL, me, 1, W);
+    const P me = (rc(ev_time(word)) << 2) | (P)vclass(ev_val(word));
+    P pv = __shfl_up_sync(FULL, me, 1, W);
     if (sub == 0) pv = prev;
-    if (v) saif_add32(acc, pv & 3u, (me >> 2) - (pv >> 2));
+    if (v) saif_add32<P>(acc, pv & 3u, (me >> 2) - (pv >> 2));
     const int last = (int)min((uint32_t)(W - 1), n_here - 1);
-    const uint32_t nx = __shfl_sync(FULL, me, last, W);
+    const P nx = __shfl_sync(FULL, me, last, W);
     if (any) prev = nx;
 }
 
@@ -1534,7 +1588,7 @@ constexpr int kCopyUnroll = GLS_COPY_UNROLL;   // entries per lane loaded ahead 
 // level scratch into the pool and add their SAIF contributions to the gate
 // output's counters.  The next segment's record is loaded while the current
 // one is copied.
-template <bool kBatch, int W>
+template <bool kBatch, int W, class Wd>
 #ifndef GLS_COPY_BLOCKS
 #define GLS_COPY_BLOCKS 5   // resident blocks per SM the copy kernel is compiled for (48 registers)
 #endif
@@ -1591,11 +1645,13 @@ __global__ void __launch_bounds__(256, GLS_COPY_BLOCKS) k_copy(const WinSet<kBat
         const CopyRec nx = fetch(s + stride, nw);
         const WinDev &w = ws.get(cw);
         const bool live = s < nseg && c.n > 0;
-        const RelClamp rc(w.t_begin, w.t_end);
-        uint32_t acc[3] = {0, 0, 0};
-        // c.cprev is a clamped absolute time: at most kMaxTime unless the
-        // window starts past every event (then it is t_begin, relative 0)
-        uint32_t prev = (rc((uint32_t)min(c.cprev, (unsigned long long)kMaxTime)) << 2) | c.pclass;
+        using P = SaifP<Wd>;
+        const RelClampT<P> rc(w.t_begin, w.t_end);
+        P acc[3] = {0, 0, 0};
+        // c.cprev is a clamped absolute time: at most the largest event time
+        // unless the window starts past every event (then it is t_begin,
+        // relative 0)
+        P prev = (rc((uint32_t)min(c.cprev, (unsigned long long)EvW<Wd>::kMax)) << 2) | c.pclass;
         const uint32_t n = live ? c.n : 0;
         // groups of one warp may have different lengths: loop to the warp's longest
         uint32_t nmax = n;
@@ -1605,14 +1661,14 @@ __global__ void __launch_bounds__(256, GLS_COPY_BLOCKS) k_copy(const WinSet<kBat
         // kCopyUnroll loads per lane go out before the stores that follow
         // them: scratch and pool never overlap, and a segment's copy costs
         // one memory round trip per W * kCopyUnroll entries, not per W
-        const uint32_t *__restrict__ sp = w.scratch + c.src;
-        uint32_t *__restrict__ dp = w.pool + dst;
+        const Wd *__restrict__ sp = reinterpret_cast<const Wd *>(w.scratch) + c.src;
+        Wd *__restrict__ dp = reinterpret_cast<Wd *>(w.pool) + dst;
         for (uint32_t i0 = 0; i0 < nmax; i0 += W * kCopyUnroll) {
-            uint32_t wd[kCopyUnroll];
+            Wd wd[kCopyUnroll];
 #pragma unroll
             for (int u = 0; u < kCopyUnroll; ++u) {
                 const uint32_t i = i0 + u * W + sub;
-                wd[u] = i < n ? __ldcs(sp + i) : 0u;   // read once: stream it past L1
+                wd[u] = i < n ? __ldcs(sp + i) : Wd(0);   // read once: stream it past L1
             }
 #pragma unroll
             for (int u = 0; u < kCopyUnroll; ++u) {
@@ -1621,7 +1677,7 @@ __global__ void __launch_bounds__(256, GLS_COPY_BLOCKS) k_copy(const WinSet<kBat
                 const uint32_t i = ib + sub;
                 const bool v = i < n;
                 if (v) dp[i] = wd[u];
-                integrate_group<W>(rc, wd[u], v, ib < n ? n - ib : 1u, ib < n, prev, acc);
+                integrate_group<W, Wd, P>(rc, wd[u], v, ib < n ? n - ib : 1u, ib < n, prev, acc);
             }
         }
 #pragma unroll
@@ -1641,7 +1697,7 @@ __global__ void __launch_bounds__(256, GLS_COPY_BLOCKS) k_copy(const WinSet<kBat
 
 // ------------------------------------------------------- stimulus SAIF
 // one warp per stimulus net; blockIdx.y is the window
-template <bool kBatch>
+template <bool kBatch, class Wd>
 __global__ void __launch_bounds__(256) k_stim_saif(const WinSet<kBatch> ws)
 {
     const WinDev &w = ws.get(blockIdx.y);
@@ -1651,13 +1707,15 @@ __global__ void __launch_bounds__(256) k_stim_saif(const WinSet<kBatch> ws)
     const uint32_t net = w.stim_nets[i];
     const uint64_t off = w.net_off[net];
     const uint32_t len = w.net_len[net];
-    const RelClamp rc(w.t_begin, w.t_end);
-    uint32_t prev = 2u;   // before the first event: X from t_begin
-    uint32_t acc[3] = {0, 0, 0};
+    using P = SaifP<Wd>;
+    const RelClampT<P> rc(w.t_begin, w.t_end);
+    P prev = 2u;   // before the first event: X from t_begin
+    P acc[3] = {0, 0, 0};
+    const Wd *pw = reinterpret_cast<const Wd *>(w.pool);
     for (uint32_t i0 = 0; i0 < len; i0 += 32) {
         const bool v = i0 + lane < len;
-        const uint32_t word = v ? w.pool[off + i0 + lane] : 0u;
-        integrate_group<32>(rc, word, v, len - i0, true, prev, acc);
+        const Wd word = v ? pw[off + i0 + lane] : Wd(0);
+        integrate_group<32, Wd, P>(rc, word, v, len - i0, true, prev, acc);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -1685,11 +1743,17 @@ __global__ void __launch_bounds__(256) k_stim_saif(const WinSet<kBatch> ws)
         }                                                        \
     } while (0)
 
-void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, cudaStream_t st)
+// Windows of 64-bit event words (times past 2^30 - 2) run one at a time
+// through the thread-per-segment kernels: the host never batches them.
+void launch_stim_saif(const WinDev *dw, const WinDev &h, uint32_t nwin, uint32_t max_stim, bool wide, cudaStream_t st)
 {
     if (!max_stim || !nwin) return;
     const dim3 grid((uint32_t)(((uint64_t)max_stim * 32 + 255) / 256), nwin);
-    GLS_DISPATCH(h, dw, nwin, (k_stim_saif<<<grid, 256, 0, st>>>(ws)));
+    if (wide) {
+        k_stim_saif<false, WideWord><<<grid, 256, 0, st>>>(WinSet<false>{h});
+        return;
+    }
+    GLS_DISPATCH(h, dw, nwin, (k_stim_saif<decltype(ws)::kIsBatch, uint32_t><<<grid, 256, 0, st>>>(ws)));
 }
 
 void launch_wave_events(const WinDev *dw, uint32_t nwin, const LevelArgs &a, cudaStream_t st)
@@ -1702,12 +1766,12 @@ void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
     GLS_DISPATCH(h, dw, nwin, (k_plan<<<nwin, 1024, 0, st>>>(ws, a)));
 }
 
-template <class WS>
+template <class Wd, class WS>
 static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
                         cudaStream_t st)
 {
     constexpr bool B = std::is_same<WS, WinSet<true>>::value;
-    if ((a.warp_mask >> cls) & 1u) {
+    if (std::is_same<Wd, uint32_t>::value && ((a.warp_mask >> cls) & 1u)) {
         const int wgrid = sm_count * 8;
         switch (cls) {
         case 0: k_sim_warp<1, B><<<wgrid, 128, 0, st>>>(ws, a, d0, d1); return;
@@ -1718,17 +1782,21 @@ static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, 
     }
     const int grid = sm_count * (cls == 0 ? GLS_SIM1_BLOCKS : (cls == 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4)));
     switch (cls) {
-    case 0: k_sim<1, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
-    case 1: k_sim<2, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
-    case 2: k_sim<3, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
-    default: k_sim<kMaxSlots, B><<<grid, 128, 0, st>>>(ws, a, d0, d1); break;
+    case 0: k_sim<1, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
+    case 1: k_sim<2, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
+    case 2: k_sim<3, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
+    default: k_sim<kMaxSlots, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
     }
 }
 
 void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,
                 int sm_count, cudaStream_t st)
 {
-    GLS_DISPATCH(h, dw, nwin, sim_kernels(ws, a, cls, d0, d1, sm_count, st));
+    if (a.wide) {
+        sim_kernels<WideWord>(WinSet<false>{h}, a, cls, d0, d1, sm_count, st);
+        return;
+    }
+    GLS_DISPATCH(h, dw, nwin, sim_kernels<uint32_t>(ws, a, cls, d0, d1, sm_count, st));
 }
 
 void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
@@ -1737,16 +1805,25 @@ void launch_link(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
     const uint64_t warps = (uint64_t)(d1 - d0) * nwin;
     if (!warps) return;
     const uint32_t blocks = (uint32_t)((warps * 32 + 255) / 256);
-    GLS_DISPATCH(h, dw, nwin, (k_link<<<blocks, 256, 0, st>>>(ws, a, d0, d1)));
+    if (a.wide) {
+        k_link<false, WideWord><<<blocks, 256, 0, st>>>(WinSet<false>{h}, a, d0, d1);
+        return;
+    }
+    GLS_DISPATCH(h, dw, nwin, (k_link<decltype(ws)::kIsBatch, uint32_t><<<blocks, 256, 0, st>>>(ws, a, d0, d1)));
 }
 
 void launch_copy(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, uint32_t d0, uint32_t d1,
                  int sm_count, cudaStream_t st)
 {
-    if (a.copy_lanes == 4) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 4><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
-    else if (a.copy_lanes == 8) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 8><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
-    else if (a.copy_lanes == 32) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 32><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
-    else GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 16><<<sm_count * 8, 256, 0, st>>>(ws, a, d0, d1)));
+    const int grid = sm_count * 8;
+    if (a.wide) {   // 8 lanes move 64 bytes a step, as 16 lanes of 32-bit words do
+        k_copy<false, 8, WideWord><<<grid, 256, 0, st>>>(WinSet<false>{h}, a, d0, d1);
+        return;
+    }
+    if (a.copy_lanes == 4) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 4, uint32_t><<<grid, 256, 0, st>>>(ws, a, d0, d1)));
+    else if (a.copy_lanes == 8) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 8, uint32_t><<<grid, 256, 0, st>>>(ws, a, d0, d1)));
+    else if (a.copy_lanes == 32) GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 32, uint32_t><<<grid, 256, 0, st>>>(ws, a, d0, d1)));
+    else GLS_DISPATCH(h, dw, nwin, (k_copy<decltype(ws)::kIsBatch, 16, uint32_t><<<grid, 256, 0, st>>>(ws, a, d0, d1)));
 }
 
 }  // namespace gls

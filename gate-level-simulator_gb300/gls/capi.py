@@ -63,7 +63,7 @@ class Stats(C.Structure):
                 ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("n_windows", C.c_uint32),
                 ("plan_ms", C.c_double), ("sim_ms", C.c_double), ("combine_ms", C.c_double),
                 ("stim_ms", C.c_double), ("fanin_bytes", C.c_uint64), ("presize_overflows", C.c_uint64),
-                ("pool_used", C.c_uint64)]
+                ("pool_used", C.c_uint64), ("wide_windows", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

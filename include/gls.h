@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define GLS_ABI_VERSION 1
+#define GLS_ABI_VERSION 2
 
 /* status codes */
 #define GLS_OK 0
@@ -148,6 +148,7 @@ typedef struct {
     uint64_t fanin_bytes;     /* fan-in event bytes the gate kernels read (5 B per event per net) */
     uint64_t presize_overflows; /* GLS_ALLOC_LEARNED: gate outputs longer than their predicted slot */
     uint64_t pool_used;       /* events allocated in the pool (stimulus + gate-output slots) */
+    uint64_t wide_windows;    /* windows run with 64-bit event words (a time past 2^30 - 2) */
 } gls_stats;
 
 /* Create a context on opts->device.  Replaces cudaSetDevice(0) and the
@@ -163,7 +164,13 @@ int gls_load_netlist(gls_ctx *ctx, const gls_netlist *nl);
 
 /* Add a stimulus window (SAIF integral over [t_begin, t_end)).  Replaces
  * VCDParser::parse/process and the per-level H2D staging of primary inputs
- * (src/simulate.cu:1974-1989, 2166-2219, 2441-2477). */
+ * (src/simulate.cu:1974-1989, 2166-2219, 2441-2477).  Event times (stimulus
+ * and gate outputs) reach 2^32 - 2, the 32-bit times of the reference GPU
+ * tool: a window whose times stay within 2^30 - 2 runs in 32-bit event
+ * words, a later time switches it to 64-bit words (twice the pool bytes;
+ * the window runs alone, never in a wave of gls_run_batched).  A stimulus
+ * time of 2^32 - 1 is GLS_ERANGE here, a gate output past 2^32 - 2 is
+ * GLS_ERANGE from the run. */
 int gls_add_window(gls_ctx *ctx, const gls_stimulus *stim, uint64_t t_begin,
                    uint64_t t_end, uint32_t *window_id);
 int gls_clear_windows(gls_ctx *ctx);

@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol(libgls):
 
 
 def test_abi_version(libgls):
-    assert libgls.gls_abi_version() == 1
+    assert libgls.gls_abi_version() == 2
 
 
 def test_create_rejects_bad_calc_mode(libgls):

@@ -191,7 +191,7 @@ def test_gpu_saif_table_matches_counts(gpu, oracle_bin):
 
 
 def test_gpu_rejects_bad_stimulus_values(gpu):
-    """A value above 3 or a time past 2^30-2 is refused when the window is added."""
+    """A value above 3 or a time of 2^32-1 is refused when the window is added."""
     nl = assemble([("GEN_INV_D1", [0], [1], [(2, "i", "zn", 5, 5)])])
     with Simulator() as s:
         s.load(nl)
@@ -200,7 +200,7 @@ def test_gpu_rejects_bad_stimulus_values(gpu):
         with pytest.raises(GlsError, match="value above 3"):
             s.add_window(bad_v, 0, 10)
         bad_t = stimulus({0: [(0, 0), (5, 3)]})
-        bad_t.time[1] = (1 << 30) - 1
+        bad_t.time[1] = (1 << 32) - 1
         with pytest.raises(GlsError, match="largest event time"):
             s.add_window(bad_t, 0, 10)
         s.add_window(stimulus({0: [(0, 0), (5, 3)]}), 0, 10)   # the context stays usable
