@@ -401,6 +401,7 @@ def gls_arm(args):
         "schedule": dict(sched, seg_events=args.seg or "auto"),
         "sim_cycles_per_s": sim_cycles,
         "gate_events_per_step": gate_ev, "output_events_per_step": stats["output_events"],
+        "fanin_events_per_step": stats["fanin_bytes"] // 5,
         "roofline": {"bound": "hbm", "kernel": "k_sim", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_basis": traffic_basis,
                      "peak_source": src,
@@ -535,6 +536,32 @@ def batched_arm(args):
     launches = sim.stats()["launches"]
     pool_b = sim.stats()["pool_bytes"]
     sim.close()
+    # The fixed cost of the launch sequence, which a persistent kernel could
+    # at most remove: the same windows cut to one cycle each, so every kernel
+    # of every level still launches (plan over all gates included) with next
+    # to no events.  Cost per launch, times this run's launches, against its
+    # device time.
+    fixed = Simulator(device=local, alloc_mode=alloc)
+    if args.alloc == "learned":
+        fixed.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
+    fixed.load(nl)
+    fixed.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"], tune["best"]["flags"])
+    one = synth.scaled(cfg, cycles=1)
+    tiny = [(synth.make_stimulus(one, nl.ppi_nets, seed=args.seed + 100 + k), one.t_end) for k in mine]
+    fixed_ms = fixed_launches = 0
+    for rep in range(3):   # the first pass warms up
+        fixed.clear_windows()
+        for st, t_end in tiny:
+            fixed.add_window(st, 0, t_end)
+        fixed.run_batched(saif_only=True)
+        fixed_ms, fixed_launches = fixed.stats()["kernel_ms"], fixed.stats()["launches"]
+    fixed.close()
+    per_launch_us = 1000.0 * fixed_ms / max(1, fixed_launches)
+    launch_cost = {"per_launch_us": per_launch_us, "launches_per_step": int(launches),
+                   "est_ms_per_step": per_launch_us * launches / 1000.0,
+                   "share_of_device_time": per_launch_us * launches / 1000.0 / (dev_ms / args.steps),
+                   "what": "device time per launch of the same windows cut to one cycle (every kernel of every "
+                           "level launched, next to no events), times this step's launches"}
     # sequential plain runs of the same windows (exact allocation, one gls_run each)
     plain = Simulator(device=local, alloc_mode=ALLOC_EXACT)
     plain.load(nl)
@@ -571,6 +598,7 @@ def batched_arm(args):
         "plain_sequential": {"value": gate_ev / plain_s, "unit": "gate-events/s", "ms": 1000.0 * plain_s,
                              "what": "the same windows as sequential gls_run calls, exact allocation, wall clock"},
         "batched_over_plain": plain_s / step_s,
+        "launch_cost": launch_cost,
         "gpu_launches": int(launches),
         "pool_bytes": pool_b,
         "clocks": clk.summary(),

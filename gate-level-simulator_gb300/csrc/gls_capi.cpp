@@ -64,6 +64,8 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->def_delay = ctx->def_delay;
     a->alloc_mode = (uint32_t)ctx->opts.alloc_mode;
     a->copy_lanes = ctx->copy_lanes;
+    a->sim_variant = ctx->sim_variant;
+    a->bal_weight = ctx->bal_weight;
     a->wave_e = nullptr;
     a->wide = 0;
 }
@@ -124,6 +126,10 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
     cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
     if (const char *v = getenv("GLS_CLASS_PRIORITY")) ctx->class_priority = strtoul(v, nullptr, 0) != 0;
     if (const char *v = getenv("GLS_WIDE_FIRST")) ctx->wide_first = strtoul(v, nullptr, 0) != 0;
+    if (const char *v = getenv("GLS_BALANCE_WEIGHT")) {   // sets the factor, and turns the balance on
+        ctx->bal_weight_on = std::max(0.f, strtof(v, nullptr));
+        ctx->bal_weight = ctx->bal_weight_on;
+    }
     for (int c = 0; c < kClasses && e == cudaSuccess; ++c) {
         // two sets: default priority, and priority rising with fan-in (a schedule option)
         const int prio = c >= 2 ? prio_hi : (c == 1 ? (prio_lo + prio_hi) / 2 : prio_lo);
@@ -815,6 +821,7 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
         if (nwin != 1) return fail(ctx, GLS_EINVAL, "64-bit event windows run one at a time");
         a.wide = 1;
         a.warp_mask = 0;
+        a.sim_variant = 0;
     }
     // Overlapped levels: every class runs simulate, link and copy on its own
     // stream; the main stream plans the next level as soon as every class
@@ -1128,6 +1135,21 @@ extern "C" int gls_run(gls_ctx *ctx)
     return GLS_OK;
 }
 
+static void apply_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask, uint32_t flags)
+{
+    ctx->seg_per_sm = seg_per_sm;
+    ctx->warp_mask = warp_mask;
+    ctx->class_priority = flags & GLS_SCHED_CLASS_PRIORITY;
+    ctx->sim_variant = ((flags & GLS_SCHED_BLOCK256) ? 1u : 0u) | ((flags & GLS_SCHED_WIDE_LOADS) ? 2u : 0u);
+    ctx->bal_weight = (flags & GLS_SCHED_LEARNED_BALANCE) ? ctx->bal_weight_on : 0.f;
+}
+
+static uint32_t schedule_flags(const gls_ctx *ctx)
+{
+    return (ctx->class_priority ? GLS_SCHED_CLASS_PRIORITY : 0u) | ((ctx->sim_variant & 1u) ? GLS_SCHED_BLOCK256 : 0u) |
+           ((ctx->sim_variant & 2u) ? GLS_SCHED_WIDE_LOADS : 0u) | (ctx->bal_weight > 0.f ? GLS_SCHED_LEARNED_BALANCE : 0u);
+}
+
 // Checks and buffers of a batched run; *B receives the windows per wave.
 static int batch_setup(gls_ctx *ctx, const gls_batch_opts &o, uint64_t *B)
 {
@@ -1195,7 +1217,7 @@ static int run_wave(gls_ctx *ctx, size_t w0, uint32_t nwin, const gls_batch_opts
     if (o.use_graph && nwin > 1) {
         // one graph per wave shape; the descriptors it reads are rewritten per wave
         gls_ctx::WaveGraph key{nwin, max_stim, ctx->warp_mask, (uint32_t)ctx->opts.alloc_mode, ctx->seg_per_sm,
-                               ctx->class_priority ? 1u : 0u, nullptr, 0};
+                               schedule_flags(ctx), nullptr, 0};
         cudaGraphExec_t ge = nullptr;
         uint32_t l = 0;
         for (auto &g : ctx->graphs)
@@ -1316,12 +1338,11 @@ extern "C" int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts)
 extern "C" int gls_set_schedule(gls_ctx *ctx, uint32_t seg_per_sm, uint32_t warp_mask, uint32_t flags)
 {
     if (!ctx) return GLS_EINVAL;
-    if (seg_per_sm < 64 || seg_per_sm > 65536 || warp_mask > 7 || flags > 1)
+    const uint32_t all = GLS_SCHED_CLASS_PRIORITY | GLS_SCHED_BLOCK256 | GLS_SCHED_WIDE_LOADS | GLS_SCHED_LEARNED_BALANCE;
+    if (seg_per_sm < 64 || seg_per_sm > 65536 || warp_mask > 7 || (flags & ~all))
         return fail(ctx, GLS_EINVAL, "schedule out of range: %u segments per SM, warp mask %u, flags %u", seg_per_sm,
                     warp_mask, flags);
-    ctx->seg_per_sm = seg_per_sm;
-    ctx->warp_mask = warp_mask;
-    ctx->class_priority = flags & GLS_SCHED_CLASS_PRIORITY;
+    apply_schedule(ctx, seg_per_sm, warp_mask, flags);
     ctx_drop_graphs(ctx);
     return GLS_OK;
 }
@@ -1336,58 +1357,59 @@ extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_r
     int rc = batch_setup(ctx, o, &B);
     if (rc) return rc;
     const uint32_t nwin = (uint32_t)std::min<uint64_t>(B, ctx->windows.size());
-    // candidates: time segments per SM for the thread-per-segment kernel, and
-    // which fan-in classes run warp-per-segment
+    // Stage 1: time segments per SM for the thread-per-segment kernel times
+    // which fan-in classes run warp-per-segment.  Stage 2, on the best of
+    // those: class-stream priority, the gate kernel's block size and load
+    // width (the variants change nothing but speed).
     static const uint32_t kSegs[] = {1024, 2048, 4096};
     static const uint32_t kMasks[] = {0, 1, 7};
-    static const uint32_t kFlags[] = {0, GLS_SCHED_CLASS_PRIORITY};
+    static const uint32_t kFlags2[] = {GLS_SCHED_CLASS_PRIORITY, GLS_SCHED_BLOCK256, GLS_SCHED_WIDE_LOADS,
+                                       GLS_SCHED_BLOCK256 | GLS_SCHED_WIDE_LOADS};
     gls_tune_result r;
     std::memset(&r, 0, sizeof r);
     float best = 1e30f;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
-    const uint32_t keep_segs = ctx->seg_per_sm, keep_mask = ctx->warp_mask;
-    const bool keep_prio = ctx->class_priority;
+    const uint32_t keep_segs = ctx->seg_per_sm, keep_mask = ctx->warp_mask, keep_flags = schedule_flags(ctx);
     uint32_t c = 0;
-    for (uint32_t f_i = 0; f_i < 2 && rc == GLS_OK; ++f_i) {
-        for (uint32_t ms_i = 0; ms_i < 3 && rc == GLS_OK; ++ms_i) {
-            for (uint32_t s_i = 0; s_i < 3 && rc == GLS_OK; ++s_i, ++c) {
-                ctx->seg_per_sm = kSegs[s_i];
-                ctx->warp_mask = kMasks[ms_i];
-                ctx->class_priority = kFlags[f_i] & GLS_SCHED_CLASS_PRIORITY;
-                RunAcc acc;
-                float t = 1e30f;
-                // the first run of a shape captures its graph; the best of the next two counts
-                for (int rep = 0; rep < 3 && rc == GLS_OK; ++rep) {
-                    float tr = 0.f;
-                    rc = run_wave(ctx, 0, nwin, o, acc, &tr, e0, e1);
-                    if (rep) t = std::min(t, tr);
-                }
-                r.ms[c] = t;
-                r.seg_per_sm[c] = kSegs[s_i];
-                r.warp_mask[c] = kMasks[ms_i];
-                r.flags[c] = kFlags[f_i];
-                if (rc == GLS_OK && t < best) {
-                    best = t;
-                    r.best = c;
-                }
-            }
+    auto trial = [&](uint32_t segs, uint32_t mask, uint32_t flags) {
+        apply_schedule(ctx, segs, mask, flags);
+        RunAcc acc;
+        float t = 1e30f;
+        // the first run of a shape captures its graph; the best of the next two counts
+        for (int rep = 0; rep < 3 && rc == GLS_OK; ++rep) {
+            float tr = 0.f;
+            rc = run_wave(ctx, 0, nwin, o, acc, &tr, e0, e1);
+            if (rep) t = std::min(t, tr);
         }
+        r.ms[c] = t;
+        r.seg_per_sm[c] = segs;
+        r.warp_mask[c] = mask;
+        r.flags[c] = flags;
+        if (rc == GLS_OK && t < best) {
+            best = t;
+            r.best = c;
+        }
+        ++c;
+    };
+    for (uint32_t ms_i = 0; ms_i < 3 && rc == GLS_OK; ++ms_i)
+        for (uint32_t s_i = 0; s_i < 3 && rc == GLS_OK; ++s_i) trial(kSegs[s_i], kMasks[ms_i], 0);
+    const uint32_t segs1 = r.seg_per_sm[r.best], mask1 = r.warp_mask[r.best];
+    for (uint32_t f : kFlags2) {
+        if (rc != GLS_OK) break;
+        trial(segs1, mask1, f);
     }
+    if (rc == GLS_OK && ctx->opts.alloc_mode == GLS_ALLOC_LEARNED) trial(segs1, mask1, GLS_SCHED_LEARNED_BALANCE);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     r.n = c;
     r.windows = nwin;
     if (rc) {
-        ctx->seg_per_sm = keep_segs;
-        ctx->warp_mask = keep_mask;
-        ctx->class_priority = keep_prio;
+        apply_schedule(ctx, keep_segs, keep_mask, keep_flags);
         return rc;
     }
-    ctx->seg_per_sm = r.seg_per_sm[r.best];
-    ctx->warp_mask = r.warp_mask[r.best];
-    ctx->class_priority = r.flags[r.best] & GLS_SCHED_CLASS_PRIORITY;
+    apply_schedule(ctx, r.seg_per_sm[r.best], r.warp_mask[r.best], r.flags[r.best]);
     if (res) *res = r;
     return GLS_OK;
 }

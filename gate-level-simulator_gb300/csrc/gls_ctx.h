@@ -230,6 +230,9 @@ struct gls_ctx {
     bool concurrent = true;
     bool wide_first = false;         // launch the widest fan-in class first (GLS_WIDE_FIRST)
     bool class_priority = false;     // wider classes on higher-priority side streams (GLS_CLASS_PRIORITY)
+    uint32_t sim_variant = 0;        // thread-per-segment gate kernel: bit 0 256-thread blocks, bit 1 wider loads
+    float bal_weight = 0.f;          // learned balance of segments in use (0: off)
+    float bal_weight_on = 0.5f;      // its factor when GLS_SCHED_LEARNED_BALANCE is set (GLS_BALANCE_WEIGHT)
     bool pipeline = true;            // with concurrent classes: each class links and copies on its own stream
     uint32_t copy_lanes = 8;         // lanes per segment of the copy kernel (GLS_COPY_LANES: 4, 8, 16, 32)
     int sm_count = 0;
@@ -275,13 +278,13 @@ struct gls_ctx {
     DevBuf wave_e;                   // per level: a wave's fan-in events per class
     std::vector<DevBuf> spare_bufs;  // device buffers of windows that ran saif_only, reused by later windows
     struct WaveGraph {
-        uint32_t nwin, max_stim, warp_mask, alloc_mode, seg_per_sm, class_priority;
+        uint32_t nwin, max_stim, warp_mask, alloc_mode, seg_per_sm, flags;   // flags: GLS_SCHED_*
         cudaGraphExec_t exec;
         uint32_t launches;
         bool same(const WaveGraph &o) const
         {
             return nwin == o.nwin && max_stim == o.max_stim && warp_mask == o.warp_mask &&
-                   alloc_mode == o.alloc_mode && seg_per_sm == o.seg_per_sm && class_priority == o.class_priority;
+                   alloc_mode == o.alloc_mode && seg_per_sm == o.seg_per_sm && flags == o.flags;
         }
     };
     std::vector<WaveGraph> graphs;

@@ -192,6 +192,8 @@ struct LevelArgs {
     uint32_t copy_lanes;        // lanes per segment in the copy kernel (4, 8, 16 or 32)
     unsigned long long *wave_e; // wave of windows: fan-in events of the level per class over all windows (else null)
     uint32_t wide;              // 1: the window holds 64-bit event words (one window per launch)
+    uint32_t sim_variant;       // thread-per-segment gate kernel variant: bit 0 256-thread blocks, bit 1 wider loads
+    float bal_weight;           // learned mode: segment work = fan-in events + bal_weight * predicted output events
 };
 
 // Windows simulated together: every level kernel takes a device array of

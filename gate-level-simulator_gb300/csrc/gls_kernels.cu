@@ -106,6 +106,13 @@ __device__ __forceinline__ uint32_t regular_delay(const NetDelay *__restrict__ n
                                                   uint32_t curp, uint32_t lastp, uint32_t defd)
 {
     uint32_t d = kInf;   // so1: the output sense minus one
+    if (M > 1 && chg != 0u && (chg & (chg - 1u)) == 0u) {
+        // one input net changed (most steps): one table entry, no loop
+        const int j = __ffs(chg) - 1;
+        const uint32_t neg = (kNegTab >> (slot_val(lastp, j) * 4 + slot_val(curp, j))) & 1u;
+        d = __ldg(&nd[j].d[neg * 4 + so1]);
+        return d == kInf ? defd : d;
+    }
 #pragma unroll
     for (int j = 0; j < M; ++j) {
         if ((chg >> j) & 1u) {
@@ -244,6 +251,8 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
     __shared__ unsigned long long sm64[32], sm64b[32], s_sum[kClasses + 1];
     __shared__ uint32_t sm32[32];
     __shared__ uint32_t s_seg[kClasses];
+    __shared__ float s_wseg[kClasses];   // learned balance: work units per segment
+    __shared__ unsigned long long s_pred[kClasses];
     __shared__ unsigned long long s_base;
     const WinDev &w = ws.get(blockIdx.x);
     const uint32_t n = a.hi - a.lo;
@@ -253,13 +262,20 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         return;
     }
     if (threadIdx.x <= kClasses) s_sum[threadIdx.x] = 0;
+    if (threadIdx.x < kClasses) s_pred[threadIdx.x] = 0;
+    // Learned balance (learned allocation): a segment's work is its fan-in
+    // events plus bal_weight times the gate output's predicted events, and
+    // segments are cut to equal work, so gates that change their output
+    // often get more, shorter segments and the lanes of a warp finish
+    // together.
+    const bool bal = a.alloc_mode == kAllocLearned && a.bal_weight > 0.f;
     // Pass 1: every gate output's fan-in events E and fan-in class, parked
     // in its slot entry as E << 2 | class until pass 2 overwrites it; the
     // level's fan-in events per
     // class (every class runs as its own launch, so every class is split
     // into about seg_target segments) and its gate events.
     const uint32_t step = blockDim.x * kPlanPer;
-    unsigned long long e_cls[kClasses] = {0, 0, 0, 0}, g_tot = 0;
+    unsigned long long e_cls[kClasses] = {0, 0, 0, 0}, p_cls[kClasses] = {0, 0, 0, 0}, g_tot = 0;
     for (uint32_t r = 0; r < n; r += step) {
 #pragma unroll
         for (int k = 0; k < kPlanPer; ++k) {
@@ -272,8 +288,9 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             for (int j = 0; j < kMaxSlots; ++j)
                 if (j < m) E += w.net_len[md.net[j]];
             const int c = fanin_class(m);
+            const unsigned long long pr = bal ? w.pred[i] : 0u;
 #pragma unroll
-            for (int q = 0; q < kClasses; ++q) if (q == c) e_cls[q] += E;
+            for (int q = 0; q < kClasses; ++q) if (q == c) { e_cls[q] += E; p_cls[q] += pr; }
             if (md.flags & kFlagFirstOut) {  // first output of its instance: count fan-in per pin
                 for (int p = 0; p < md.n_pins; ++p) g_tot += w.net_len[md.net[(md.pin_slot >> (3 * p)) & 7u]];
             }
@@ -289,6 +306,15 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
             if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_sum[q], v);
+        }
+        if (bal) {
+#pragma unroll
+            for (int q = 0; q < kClasses; ++q) {
+                unsigned long long v = p_cls[q];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
+                if ((threadIdx.x & 31) == 0 && v) atomicAdd(&s_pred[q], v);
+            }
         }
     }
     __syncthreads();
@@ -309,6 +335,8 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             const unsigned long long ev = a.wave_e ? a.wave_e[k] : s_sum[k];   // the wave shares the GPU
             if (!seg) seg = max(warp ? 128ull : 32ull, (ev + target - 1) / max(1ull, target));
             s_seg[k] = (uint32_t)min(max(seg, floor_seg), 0x7FFFFFFFull);
+            // as many segments in the class as without the balance
+            s_wseg[k] = (float)s_seg[k] * (1.f + a.bal_weight * (float)s_pred[k] / (float)max(1ull, s_sum[k]));
         }
         s_base = *w.top;
         atomicAdd(&w.counters[0], s_sum[kClasses]);
@@ -334,6 +362,12 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
             const unsigned long long E = ec >> 2;
             const uint32_t seg = s_seg[ec & 3u];
             S = (uint32_t)max(1ull, (E + seg - 1) / seg);
+            if (bal && E > 0) {
+                const float work = (float)E + a.bal_weight * (float)w.pred[i];
+                const float sf = ceilf(work / s_wseg[ec & 3u]);
+                // at most one segment per fan-in event, and within the segment floor's count
+                S = (uint32_t)min((float)E, max(1.f, min(sf, (float)((E + seg - 1) / seg) * 4.f)));
+            }
             slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
             if (a.alloc_mode == kAllocExact) slot = 0;
             else if (a.alloc_mode == kAllocLearned) slot = min(slot, ((unsigned long long)w.pred[i] + 3) & ~3ull);
@@ -427,7 +461,15 @@ __device__ __forceinline__ uint32_t sel4(const uint4 &q, uint32_t k)
 #ifndef GLS_SIM_WARP_BATCH
 #define GLS_SIM_WARP_BATCH 1   // thread-per-segment kernels: a warp takes 32 segments at a time
 #endif
-constexpr uint32_t kSimBlock = 128;   // threads per block of the thread-per-segment kernels
+// Threads per block of the thread-per-segment kernels: 128, or 256 in the
+// kernel variants with bit kSimV256 (as many threads resident per SM: half
+// the blocks, each balancing its segments over twice the warps).  Variants
+// with bit kSimVWide read twice the events per load (4 for 1- and 2-input
+// gates, 2 for wider ones: fewer loads, more registers).  The autotuner picks
+// the variant; 64-bit windows always run variant 0.
+constexpr uint32_t kSimBlock = 128;
+constexpr int kSimV256 = 1, kSimVWide = 2;
+template <int kV> constexpr uint32_t sim_block() { return (kV & kSimV256) ? 256u : kSimBlock; }
 #ifndef GLS_READER_W3
 #define GLS_READER_W3 1   // events per reader chunk in the wider gate kernels
 #endif
@@ -639,12 +681,12 @@ __device__ __forceinline__ void cut_at(const Wd *__restrict__ pool, const uint64
     }
 }
 
-template <int M, class Wd>
+template <int M, class Wd, bool kWideChunk>
 __device__ void sim_segment(const WinDev &w, const LevelArgs &a, const DrvMeta &md, uint32_t s,
                             uint32_t S, uint32_t seg_id, uint64_t scr, const uint4 sl)
 {
     constexpr bool kSlut = M <= 3;   // truth table in registers
-    constexpr int kRW = M >= 3 ? GLS_READER_W3 : GLS_READER_W2;   // events per reader chunk
+    constexpr int kRW = (M >= 3 ? GLS_READER_W3 : GLS_READER_W2) * (kWideChunk ? 2 : 1);   // events per reader chunk
     // 64-bit words (a window with times past 2^30 - 2) are read one at a time
     using RD = typename std::conditional<std::is_same<Wd, uint32_t>::value, Reader<kRW>, ReaderWide>::type;
     using RC = typename RD::C;
@@ -801,7 +843,7 @@ __device__ __forceinline__ uint32_t window_of(const uint32_t *s_pre, uint32_t nw
 // owns a contiguous share of the class's segments and its threads take the
 // next one from a shared counter as they finish, so long and short segments
 // balance inside the block.
-template <int M, bool kBatch, class Wd>
+template <int M, bool kBatch, class Wd, int kV>
 #ifndef GLS_SIM2_BLOCKS
 #define GLS_SIM2_BLOCKS 8   // resident blocks per SM the 1- and 2-input gate kernels are compiled for
 #endif
@@ -811,7 +853,8 @@ template <int M, bool kBatch, class Wd>
 #ifndef GLS_SIM1_BLOCKS
 #define GLS_SIM1_BLOCKS GLS_SIM2_BLOCKS   // resident blocks per SM the 1-input gate kernel is compiled for
 #endif
-__global__ void __launch_bounds__(kSimBlock, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4)))
+__global__ void __launch_bounds__(sim_block<kV>(), (M == 1 ? GLS_SIM1_BLOCKS : (M == 2 ? GLS_SIM2_BLOCKS : (M == 3 ? GLS_SIM3_BLOCKS : 4))) /
+                                                    ((kV & kSimV256) ? 2 : 1))
     k_sim(const WinSet<kBatch> ws, LevelArgs a, uint32_t d0, uint32_t d1)
 {
     __shared__ uint32_t s_next;
@@ -884,7 +927,7 @@ __global__ void __launch_bounds__(kSimBlock, M == 1 ? GLS_SIM1_BLOCKS : (M == 2 
         const uint32_t S = w.seg_base[i + 1] - sb;
         const DrvMeta md = a.meta[a.lo + i];
         const uint4 sl = M <= 3 ? __ldg(a.slut + a.lo + i) : make_uint4(0, 0, 0, 0);
-        sim_segment<M, Wd>(w, a, md, g - sb, S, g, w.scr[i], sl);
+        sim_segment<M, Wd, (kV & kSimVWide) != 0>(w, a, md, g - sb, S, g, w.scr[i], sl);
     }
 }
 
@@ -1766,6 +1809,24 @@ void launch_plan(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelAr
     GLS_DISPATCH(h, dw, nwin, (k_plan<<<nwin, 1024, 0, st>>>(ws, a)));
 }
 
+// one block per resident slot of every SM
+template <class Wd, int kV, class WS>
+static void sim_thread(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
+                       cudaStream_t st)
+{
+    constexpr bool B = std::is_same<WS, WinSet<true>>::value;
+    constexpr uint32_t bs = sim_block<kV>();
+    const int per_sm = (cls == 0 ? GLS_SIM1_BLOCKS : (cls == 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4))) /
+                       ((kV & kSimV256) ? 2 : 1);
+    const int grid = sm_count * per_sm;
+    switch (cls) {
+    case 0: k_sim<1, B, Wd, kV><<<grid, bs, 0, st>>>(ws, a, d0, d1); break;
+    case 1: k_sim<2, B, Wd, kV><<<grid, bs, 0, st>>>(ws, a, d0, d1); break;
+    case 2: k_sim<3, B, Wd, kV><<<grid, bs, 0, st>>>(ws, a, d0, d1); break;
+    default: k_sim<kMaxSlots, B, Wd, kV><<<grid, bs, 0, st>>>(ws, a, d0, d1); break;
+    }
+}
+
 template <class Wd, class WS>
 static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1, int sm_count,
                         cudaStream_t st)
@@ -1780,13 +1841,15 @@ static void sim_kernels(const WS &ws, const LevelArgs &a, int cls, uint32_t d0, 
         default: break;
         }
     }
-    const int grid = sm_count * (cls == 0 ? GLS_SIM1_BLOCKS : (cls == 1 ? GLS_SIM2_BLOCKS : (cls == 2 ? GLS_SIM3_BLOCKS : 4)));
-    switch (cls) {
-    case 0: k_sim<1, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
-    case 1: k_sim<2, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
-    case 2: k_sim<3, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
-    default: k_sim<kMaxSlots, B, Wd><<<grid, kSimBlock, 0, st>>>(ws, a, d0, d1); break;
+    if constexpr (std::is_same<Wd, uint32_t>::value) {
+        switch (a.sim_variant) {
+        case 1: sim_thread<Wd, 1>(ws, a, cls, d0, d1, sm_count, st); return;
+        case 2: sim_thread<Wd, 2>(ws, a, cls, d0, d1, sm_count, st); return;
+        case 3: sim_thread<Wd, 3>(ws, a, cls, d0, d1, sm_count, st); return;
+        default: break;
+        }
     }
+    sim_thread<Wd, 0>(ws, a, cls, d0, d1, sm_count, st);
 }
 
 void launch_sim(const WinDev *dw, const WinDev &h, uint32_t nwin, const LevelArgs &a, int cls, uint32_t d0, uint32_t d1,

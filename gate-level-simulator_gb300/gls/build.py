@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", f"-I{REPO / 'include'}", f"-I{CSRC}"]
 
 LIB_SOURCES = ["gls_kernels.cu", "gls_capi.cpp", "gls_cells.cpp", "gls_static.cu", "gls_presize.cu",
-               "gls_levelize.cu", "gls_vcd.cu"]
+               "gls_levelize.cu", "gls_vcd.cu", "gls_pack.cu"]
 
 
 def nvcc() -> str:

@@ -29,7 +29,7 @@ EXPORTED = ["gls_create", "gls_destroy", "gls_last_error", "gls_load_netlist", "
             "gls_set_presize_model", "gls_presize_samples", "gls_presize_predict", "gls_trainer_create",
             "gls_trainer_destroy", "gls_trainer_error", "gls_trainer_set_data", "gls_trainer_fit",
             "gls_trainer_grad", "gls_trainer_get_params", "gls_trainer_set_params", "gls_run_batched",
-            "gls_autotune", "gls_set_schedule", "gls_levelize", "gls_vcd_scan", "gls_vcd_free"]
+            "gls_autotune", "gls_set_schedule", "gls_levelize", "gls_vcd_scan", "gls_vcd_free", "gls_pack_levels"]
 
 
 class GlsError(RuntimeError):
@@ -193,6 +193,72 @@ def levelize_gpu(pred_start: np.ndarray, pred: np.ndarray, device: int = 0):
     if rc:
         raise GlsError(rc, "gls_levelize: malformed predecessor table or combinational loop")
     return order[:n], level_start[: nl.value + 1]
+
+
+PACK_ARC_DTYPE = np.dtype([("edge", "<i2"), ("in_pos", "<i2"), ("out_pos", "<i2"), ("pad", "<i2"),
+                           ("rise", "<f4"), ("fall", "<f4")])
+
+
+class PackIn(C.Structure):
+    _fields_ = [("n_levels", C.c_uint32), ("n_inst", C.c_uint32)] + \
+               [(f, C.c_void_p) for f in ("level_start", "n_in", "n_out", "arc_start", "arcs", "row_start",
+                                          "entry_start", "entries")]
+
+
+PACK_LEVEL = ("data_in_num_start", "data_out_num_start", "delay_start", "delay_width", "functions_start",
+              "functions_width")
+PACK_INST = (("data_in_num", np.int16), ("data_out_num", np.int16), ("val_num_start", np.uint32),
+             ("delay_val_num", np.int16), ("functions_func_num", np.int16), ("functions_val_num", np.int16))
+PACK_DELAY = (("delay_edges", np.int16), ("in_bit", np.int16), ("out_bit", np.int16), ("rise_val", np.float32),
+              ("fall_val", np.float32))
+
+
+class PackOut(C.Structure):
+    _fields_ = [(f, C.c_void_p) for f in PACK_LEVEL] + [(f, C.c_void_p) for f, _ in PACK_INST] + \
+               [(f, C.c_void_p) for f, _ in PACK_DELAY] + [("functions", C.c_void_p)] + \
+               [(f, C.c_uint64) for f in ("delay_cap", "functions_cap", "delay_total", "functions_total")]
+
+
+def pack_levels_gpu(level_start, n_in, n_out, arc_start, arcs, row_start, entry_start, entries, device: int = 0):
+    """The reference's packed per-level arrays (gls_pack_levels) of
+    instances in level order; returns a dict of numpy arrays named as the
+    reference's fields (host_* for the padded tables).  The first call
+    sizes the padded tables, the second fills them."""
+    lib = load_library()
+    lib.gls_pack_levels.argtypes = [C.c_int, C.POINTER(PackIn), C.POINTER(PackOut)]
+    keep = dict(level_start=np.ascontiguousarray(level_start, np.uint32), n_in=np.ascontiguousarray(n_in, np.uint16),
+                n_out=np.ascontiguousarray(n_out, np.uint16), arc_start=np.ascontiguousarray(arc_start, np.uint32),
+                arcs=np.ascontiguousarray(arcs, PACK_ARC_DTYPE), row_start=np.ascontiguousarray(row_start, np.uint32),
+                entry_start=np.ascontiguousarray(entry_start, np.uint32),
+                entries=np.ascontiguousarray(entries, np.int16))
+    nl, n = len(keep["level_start"]) - 1, len(keep["n_in"])
+    pin = PackIn(nl, n, *[_ptr(keep[f]) if len(keep[f]) else None for f in
+                          ("level_start", "n_in", "n_out", "arc_start", "arcs", "row_start", "entry_start",
+                           "entries")])
+    res = {f: np.zeros(max(nl, 1), np.uint32) for f in PACK_LEVEL}
+    res.update({f: np.zeros(max(n, 1), t) for f, t in PACK_INST})
+    out = PackOut()
+    for f in PACK_LEVEL + tuple(f for f, _ in PACK_INST):
+        setattr(out, f, _ptr(res[f]))
+    rc = lib.gls_pack_levels(device, C.byref(pin), C.byref(out))
+    if rc == GLS_EOVERFLOW:   # the padded tables' sizes are known now
+        nd, nf = out.delay_total, out.functions_total
+        for f, t in PACK_DELAY:
+            res[f] = np.zeros(max(nd, 1), t)
+            setattr(out, f, _ptr(res[f]))
+        res["functions"] = np.zeros(max(nf, 1), np.int16)
+        out.functions = _ptr(res["functions"])
+        out.delay_cap, out.functions_cap = nd, nf
+        rc = lib.gls_pack_levels(device, C.byref(pin), C.byref(out))
+    if rc:
+        raise GlsError(rc, "gls_pack_levels")
+    nd, nf = out.delay_total, out.functions_total
+    r = {f: res[f][:nl] for f in PACK_LEVEL}
+    r.update({f: res[f][:n] for f, _ in PACK_INST})
+    r.update({"host_" + f if f in ("delay_edges", "in_bit", "out_bit", "rise_val", "fall_val") else f:
+              res[f][:nd] if f in res else np.zeros(0, t) for f, t in PACK_DELAY})
+    r["host_functions"] = res["functions"][:nf] if "functions" in res else np.zeros(0, np.int16)
+    return r
 
 
 class VcdIds(C.Structure):

@@ -155,6 +155,57 @@ def write_vcd(path, nl: Netlist, st: Stimulus, top: str = "top") -> None:
     Path(path).write_text("\n".join(head + body) + "\n")
 
 
+def write_stim_bin(path, nl: Netlist, st: Stimulus, time_res: int = 1, time_unit: str = "ps") -> None:
+    """The stimulus as the tools' binary stimulus file (layout in
+    host/vcd.h), the same bytes gls_vcd2stim writes for write_vcd's file:
+    one scalar signal per stimulus net, named as the netlist names it."""
+    names = [nl.net_name(int(n)) for n in st.nets]
+    out = bytearray(b"GLSSTIM1")
+    out += struct.pack("<III", time_res, len(names), len(names))
+    u = time_unit.encode()
+    out += struct.pack("<I", len(u)) + u
+    for nm in names:
+        b = nm.encode()
+        out += struct.pack("<I", len(b)) + b
+    for nm in names:
+        b = nm.encode()
+        out += struct.pack("<I", len(b)) + b + b"\x00"
+    out += np.asarray(st.ev_start, "<u8").tobytes()
+    out += np.asarray(st.time, "<u8").tobytes()
+    out += np.asarray(st.value, "u1").tobytes()
+    Path(path).write_bytes(bytes(out))
+
+
+def read_stim_bin(path):
+    """A binary stimulus file as (time_res, time_unit, names, decl_bits,
+    start, time, value); decl_bits is a list of (name, bus)."""
+    b = Path(path).read_bytes()
+    if b[:8] != b"GLSSTIM1":
+        raise ValueError("not a GLSSTIM1 file")
+    res, ns, nd = struct.unpack_from("<III", b, 8)
+    off = 20
+
+    def s():
+        nonlocal off
+        (k,) = struct.unpack_from("<I", b, off)
+        off += 4 + k
+        return b[off - k: off].decode()
+
+    unit = s()
+    names = [s() for _ in range(ns)]
+    decls = []
+    for _ in range(nd):
+        nm = s()
+        decls.append((nm, b[off] != 0))
+        off += 1
+    start = np.frombuffer(b, "<u8", ns + 1, off)
+    off += 8 * (ns + 1)
+    total = int(start[-1])
+    time = np.frombuffer(b, "<u8", total, off)
+    value = np.frombuffer(b, "u1", total, off + 8 * total)
+    return res, unit, names, decls, start, time, value
+
+
 def read_inter(path):
     """The native inter.dat of gls_process as a dict of plain arrays."""
     b = Path(path).read_bytes()

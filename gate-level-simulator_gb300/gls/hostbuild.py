@@ -1,5 +1,6 @@
-"""Build of the command-line tools gls_process and gls_simulate (C++,
-host only) into gate-level-simulator_gb300/bin, linked against libgls."""
+"""Build of the command-line tools gls_process, gls_simulate and
+gls_vcd2stim (C++, host only) into gate-level-simulator_gb300/bin, linked
+against libgls."""
 from __future__ import annotations
 
 import subprocess
@@ -10,8 +11,9 @@ from .build import BIN_DIR, LIB, LIB_DIR, PKG, REPO
 
 HOST = PKG / "host"
 TOOLS = {
-    "gls_process": ["design.cpp", "boost_inter.cpp", "gls_process.cpp"],
-    "gls_simulate": ["design.cpp", "boost_inter.cpp", "vcd.cpp", "gls_simulate.cpp"],
+    "gls_process": ["design.cpp", "boost_inter.cpp", "pack_gpu.cpp", "gls_process.cpp"],
+    "gls_simulate": ["design.cpp", "boost_inter.cpp", "vcd.cpp", "stim_bin.cpp", "gls_simulate.cpp"],
+    "gls_vcd2stim": ["design.cpp", "boost_inter.cpp", "vcd.cpp", "stim_bin.cpp", "gls_vcd2stim.cpp"],
 }
 
 

@@ -589,7 +589,7 @@ ref::ModuleType module_of(const Cell &c)
 
 }  // namespace
 
-void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out)
+void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out, bool pack)
 {
     out = ref::Inter();
     ref::PreProcess &p = out.p;
@@ -822,7 +822,16 @@ void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out)
                 if (!out.out_maps[L].count(cur.out_net[k]))
                     out.out_maps[L][cur.out_net[k]] = {(uint32_t)j, (uint32_t)k};
         }
-    // packed per-level arrays (src/process.cpp:423-566)
+    if (pack) pack_levels(out);
+}
+
+// The packed per-level arrays of an archived design (src/process.cpp:423-566).
+void pack_levels(ref::Inter &out)
+{
+    ref::PreProcess &p = out.p;
+    auto inst = [&](int id) -> ref::Instance & { return p.instances.at(p.instance_name_vec[id]); };
+    size_t n = 0;   // instances over all levels
+    for (auto &lv : out.levels) n += lv.size();
     const size_t nl = out.levels.size();
     out.data_in_num_start.assign(nl, 0);
     out.data_out_num_start.assign(nl, 0);

@@ -114,7 +114,14 @@ bool load_boost_inter(const std::string &text, ref::Inter &out, std::string *err
 // the library's modules, every instance with its connections, function
 // programs, delays and driver references, the level lists and the packed
 // per-level arrays.
-void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out);
+// pack = false leaves the packed per-level arrays empty (for pack_levels or
+// pack_levels_gpu to fill).
+void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out, bool pack = true);
+// The packed per-level arrays (src/process.cpp:423-566) from the levels and
+// instances of `out`, on the host or on GPU `device` (gls_pack_levels;
+// false with a message on a library error).
+void pack_levels(ref::Inter &out);
+bool pack_levels_gpu(ref::Inter &out, int device, std::string *err);
 // The simulation model of an archived design: instances in level order
 // with their function programs, arcs, constants, assign aliases and
 // declared bus bits.

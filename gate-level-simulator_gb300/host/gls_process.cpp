@@ -1,4 +1,4 @@
-// gls_process [--gpu-levelize] [--native] <vlib> <gv> <sdf> <inter.dat>
+// gls_process [--gpu-levelize] [--gpu-pack] [--native] <vlib> <gv> <sdf> <inter.dat>
 //
 // The `process` step of the reference (src/process.cpp:178-610): read the
 // Verilog cell library, the flat gate-level netlist and the SDF file,
@@ -6,7 +6,9 @@
 // as the reference does, a Boost text archive of its `inter` class
 // (host/boost_inter.cpp); --native writes the tools' own binary format
 // instead (host/design.cpp).  With --gpu-levelize the levels are computed
-// on GPU 0 (gls_levelize); the file is the same.
+// on GPU 0 (gls_levelize), with --gpu-pack the archive's packed per-level
+// arrays (gls_pack_levels); the file is the same.
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -18,15 +20,17 @@
 
 int main(int argc, char **argv)
 {
-    bool gpu = false, native = false;
+    bool gpu = false, gpu_pack = false, native = false;
     std::vector<char *> pos;
     for (int k = 1; k < argc; ++k) {
         if (!strcmp(argv[k], "--gpu-levelize")) gpu = true;
+        else if (!strcmp(argv[k], "--gpu-pack")) gpu_pack = true;
         else if (!strcmp(argv[k], "--native")) native = true;
         else pos.push_back(argv[k]);
     }
     if (pos.size() != 4) {
-        printf("[USAGE] ./gls_process [--gpu-levelize] [--native] vlib_path gv_path sdf_path intermediate_file\n");
+        printf("[USAGE] ./gls_process [--gpu-levelize] [--gpu-pack] [--native] vlib_path gv_path sdf_path "
+               "intermediate_file\n");
         return 255;
     }
     argv = pos.data() - 1;
@@ -83,7 +87,18 @@ int main(int argc, char **argv)
         }
     } else {
         ref::Inter in;
-        design_to_ref_inter(d, lib, in);
+        design_to_ref_inter(d, lib, in, false);
+        const auto t0 = std::chrono::steady_clock::now();
+        if (gpu_pack) {
+            if (!pack_levels_gpu(in, 0, &err)) {
+                printf("ERROR: %s\n", err.c_str());
+                return 255;
+            }
+        } else {
+            pack_levels(in);
+        }
+        printf("INFO: level packing done on the %s (%.1f ms)\n", gpu_pack ? "GPU" : "host",
+               std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
         std::ofstream f(argv[4], std::ios::binary);
         const std::string text = save_boost_inter(in);
         f.write(text.data(), (std::streamsize)text.size());

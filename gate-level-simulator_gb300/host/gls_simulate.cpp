@@ -1,4 +1,4 @@
-// gls_simulate <inter.dat> <vcd> <dumpon_time> <dumpoff_time> <out.saif>
+// gls_simulate <inter.dat> <vcd|stim> <dumpon_time> <dumpoff_time> <out.saif>
 //              [--calc fixed|literal] [--device N] [--host-vcd]
 //              [--saif-order=ref|net]
 //
@@ -16,7 +16,9 @@
 // containers it replays (host/boost_inter.cpp, saif_ref_order).
 //
 // The VCD body is scanned on the GPU (gls_vcd_scan) unless --host-vcd is
-// given; both read the same changes.
+// given; both read the same changes.  A binary stimulus file written by
+// gls_vcd2stim (it starts "GLSSTIM1") may stand in for the VCD: its change
+// lists are loaded as they are.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -102,7 +104,9 @@ int main(int argc, char **argv)
     }
     VcdData vcd;
     const std::string vtext = read_file(argv[2], &err);
-    if (vtext.empty() || (host_vcd ? !parse_vcd(vtext, vcd, &err) : parse_vcd_gpu(vtext, vcd, &err, device) < 0)) {
+    if (vtext.empty() ||
+        (is_stim_bin(vtext) ? !load_stim_bin(vtext, vcd, &err)
+                            : (host_vcd ? !parse_vcd(vtext, vcd, &err) : parse_vcd_gpu(vtext, vcd, &err, device) < 0))) {
         printf("Parse Failed. %s\n", err.c_str());
         return 1;
     }

@@ -31,4 +31,17 @@ bool parse_vcd(const std::string &text, VcdData &v, std::string *err);
 // failed scan), -1 on an error in the header.
 int parse_vcd_gpu(const std::string &text, VcdData &v, std::string *err, int device);
 
+// Binary stimulus file: a VcdData as read from a VCD, stored so that a run
+// loads it with a few large reads instead of parsing text.  Little endian:
+//   "GLSSTIM1"
+//   u32 time_res, u32 n_signals, u32 n_decl, u32 unit_len, char unit[unit_len]
+//   per signal: u32 len, char name[len]
+//   per declared bit: u32 len, char name[len], u8 bus
+//   u64 start[n_signals + 1]          (first change of each signal)
+//   u64 time[start[n_signals]]        (strictly increasing within a signal)
+//   u8  value[start[n_signals]]       (0, 1=X, 2=Z, 3)
+bool is_stim_bin(const std::string &bytes);
+std::string save_stim_bin(const VcdData &v);
+bool load_stim_bin(const std::string &bytes, VcdData &v, std::string *err);
+
 }  // namespace glsh

@@ -192,13 +192,21 @@ typedef struct {
 int gls_run_batched(gls_ctx *ctx, const gls_batch_opts *opts);
 
 /* Autotuner: runs the first wave of the added windows (as gls_run_batched
- * would form it; a single window works too) under every candidate schedule
- * -- time segments per SM for the thread-per-segment gate kernel (1024,
- * 2048, 4096) times the fan-in classes that run warp-per-segment (none,
- * 1-input, 1- to 3-input) times plain or priority class streams -- and keeps
- * the fastest for the context's later runs.  Results never depend on the
- * schedule. */
+ * would form it; a single window works too) under candidate schedules and
+ * keeps the fastest for the context's later runs: first time segments per
+ * SM for the thread-per-segment gate kernel (1024, 2048, 4096) times the
+ * fan-in classes that run warp-per-segment (none, 1-input, 1- to 3-input),
+ * then, on the best of those, each of priority class streams, 256-thread
+ * gate-kernel blocks, wider event loads, and both of the last two (13
+ * candidates), and with GLS_ALLOC_LEARNED the learned balance of segments
+ * (14).  Results never depend on the schedule. */
 #define GLS_SCHED_CLASS_PRIORITY 1u   /* wider fan-in classes on higher-priority streams */
+#define GLS_SCHED_BLOCK256 2u         /* thread-per-segment gate kernels in blocks of 256 threads (else 128) */
+#define GLS_SCHED_WIDE_LOADS 4u       /* thread-per-segment gate kernels load 4 events at a time for 1- and
+                                         2-input gates, 2 for wider ones (else 2 and 1) */
+#define GLS_SCHED_LEARNED_BALANCE 8u  /* GLS_ALLOC_LEARNED: segments cut to equal predicted work, fan-in
+                                         events plus half the presize network's predicted output events
+                                         (GLS_BALANCE_WEIGHT sets another factor) */
 typedef struct {
     uint32_t n;               /* candidates tried */
     uint32_t best;            /* index of the one kept */
@@ -242,9 +250,56 @@ int gls_cell_lut(const gls_cell *cell, const gls_prim *prims, int out,
 
 int gls_abi_version(void);
 
+/* The reference's packed per-level arrays (src/process.cpp:423-566),
+ * computed on device `device`: the tables `process` archives for its GPU
+ * simulator.  Instances are given in level order: level L holds
+ * [level_start[L], level_start[L + 1]).  Per instance: its input and output
+ * net counts, its delay arcs (arc_start CSR into arcs: the edge, the arc's
+ * input and output as positions in the instance's input / output net lists
+ * (the list's length when absent) and the rise / fall values) and its
+ * function program (row_start CSR into rows; row r holds the entries
+ * [entry_start[r], entry_start[r + 1]) of entries).
+ *
+ * Outputs, as the reference fills them (per level: starts and widths; per
+ * instance: counts; padded per level: delay and function tables, -1 where
+ * an instance has fewer entries than its level's width).  The padded
+ * tables need delay_total and functions_total entries: a call whose caps
+ * are smaller writes the two totals and returns GLS_EOVERFLOW, so a caller
+ * may size them with a first call. */
+typedef struct {
+    int16_t edge, in_pos, out_pos, pad;
+    float rise, fall;
+} gls_pack_arc;
+typedef struct {
+    uint32_t n_levels, n_inst;
+    const uint32_t *level_start;     /* n_levels + 1 */
+    const uint16_t *n_in, *n_out;    /* n_inst */
+    const uint32_t *arc_start;       /* n_inst + 1 */
+    const gls_pack_arc *arcs;
+    const uint32_t *row_start;       /* n_inst + 1 */
+    const uint32_t *entry_start;     /* rows + 1 */
+    const int16_t *entries;
+} gls_pack_in;
+typedef struct {
+    /* n_levels each */
+    uint32_t *data_in_num_start, *data_out_num_start, *delay_start, *delay_width, *functions_start,
+        *functions_width;
+    /* n_inst each */
+    int16_t *data_in_num, *data_out_num;
+    uint32_t *val_num_start;
+    int16_t *delay_val_num, *functions_func_num, *functions_val_num;
+    /* delay_cap entries each */
+    int16_t *delay_edges, *in_bit, *out_bit;
+    float *rise_val, *fall_val;
+    int16_t *functions;              /* functions_cap entries */
+    uint64_t delay_cap, functions_cap;
+    uint64_t delay_total, functions_total;   /* written */
+} gls_pack_out;
+int gls_pack_levels(int device, const gls_pack_in *in, gls_pack_out *out);
+
 /* Kahn levels of an instance graph, computed on device `device` (replaces
  * GenerateAdjacencyList / SetInDegrees / TopologyOrder, src/process.cpp:
- * 90-176, and the level packing of 423-566).  pred_start[n_inst + 1]
+ * 90-176; gls_pack_levels does the packing of 423-566).  pred_start[n_inst + 1]
  * (pred_start[0] = 0, nondecreasing) and pred[] list every instance's
  * predecessors: the instances driving its input nets (repeats are
  * harmless).  Level 0 holds the instances without predecessors; every

@@ -125,7 +125,14 @@ def test_autotune_keeps_results(design, gpu):
         s.load(nl)
         ids = [s.add_window(st, 0, t_end) for st, t_end in wins]
         t = s.autotune(max_wave=4)
-        assert len(t["candidates"]) == 18 and t["windows"] == 4
+        # 9 in the first stage, 4 flag sets on the best of them
+        assert len(t["candidates"]) == 13 and t["windows"] == 4
+        first = t["candidates"][:9]
+        stage1 = min(first, key=lambda c: c["ms"])
+        assert all(c["flags"] == 0 for c in first)
+        assert [c["flags"] for c in t["candidates"][9:]] == [1, 2, 4, 6]
+        assert all((c["seg_per_sm"], c["warp_mask"]) == (stage1["seg_per_sm"], stage1["warp_mask"])
+                   for c in t["candidates"][9:])
         assert t["best"]["ms"] == min(c["ms"] for c in t["candidates"])
         s.run_batched(max_wave=4)
         for w, (la, sa) in zip(ids, ref):

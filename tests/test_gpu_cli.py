@@ -251,3 +251,42 @@ def test_cli_hand_written_archive_matches_oracle(tools, tmp_path):
     assert recs["z"] == recs["n1"]
     assert recs["bus[1]"] == recs["bus[0]"] == (0, 0, 1000)
     assert set(recs) == {"a", "n1", "y", "k", "z", "bus[1]", "bus[0]"}
+
+
+def test_cli_binary_stimulus_gives_the_same_saif(tools, tmp_path):
+    """gls_simulate on the binary stimulus that gls_vcd2stim writes (its
+    GPU scan, and the host reader) and on the one gls.files.write_stim_bin
+    writes: the same SAIF file as on the VCD, with and without the
+    reference order; buses, aliases and constants included."""
+    from gls import hostbuild
+    tools = hostbuild.build()
+    files.write_vlib(tmp_path / "lib.vlib")
+    (tmp_path / "d.gv").write_text(GV)
+    (tmp_path / "d.sdf").write_text(SDF)
+    (tmp_path / "d.vcd").write_text(VCD)
+    r = subprocess.run([str(tools["gls_process"]), str(tmp_path / "lib.vlib"), str(tmp_path / "d.gv"),
+                        str(tmp_path / "d.sdf"), str(tmp_path / "a.dat")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    for extra, name in (([], "g.stim"), (["--host-vcd"], "h.stim")):
+        r = subprocess.run([str(tools["gls_vcd2stim"]), str(tmp_path / "d.vcd"), str(tmp_path / name), *extra],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stdout
+    assert (tmp_path / "g.stim").read_bytes() == (tmp_path / "h.stim").read_bytes()
+    for order in ([], ["--saif-order=ref"]):
+        v = simulate(tools, tmp_path / "a.dat", tmp_path / "d.vcd", 50, 1000, tmp_path / "v.saif", order)
+        b = simulate(tools, tmp_path / "a.dat", tmp_path / "g.stim", 50, 1000, tmp_path / "b.saif", order)
+        assert v == b
+    # a generated design: the Python writer's file against the VCD
+    cfg = synth.scaled(synth.CONFIGS["c1"], cells=800, cycles=200, depth=10)
+    nl0 = synth.make_netlist(cfg, 9)
+    st0 = synth.make_stimulus(cfg, nl0.ppi_nets, 10)
+    files.write_gv(tmp_path / "e.gv", nl0)
+    files.write_sdf(tmp_path / "e.sdf", nl0)
+    files.write_vcd(tmp_path / "e.vcd", nl0, st0)
+    files.write_stim_bin(tmp_path / "e.stim", nl0, st0)
+    r = subprocess.run([str(tools["gls_process"]), str(tmp_path / "lib.vlib"), str(tmp_path / "e.gv"),
+                        str(tmp_path / "e.sdf"), str(tmp_path / "e.dat")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    v = simulate(tools, tmp_path / "e.dat", tmp_path / "e.vcd", 5_000, cfg.t_end, tmp_path / "ev.saif")
+    b = simulate(tools, tmp_path / "e.dat", tmp_path / "e.stim", 5_000, cfg.t_end, tmp_path / "eb.saif")
+    assert v == b

@@ -83,12 +83,14 @@ def test_gpu_pool_offsets_past_2_34_events(gpu, oracle_bin):
 @pytest.mark.parametrize("knobs", [{"GLS_SIM_CONCURRENT": "0"}, {"GLS_SIM_PIPELINE": "0"}, {"GLS_PLAN_OVERLAP": "0"},
                                    {"GLS_COPY_LANES": "4"}, {"GLS_COPY_LANES": "16"}, {"GLS_COPY_LANES": "32"},
                                    {"profile": True}, {"schedule": (512, 7, 0)}, {"schedule": (8192, 1, 1)},
-                                   {"schedule": (2048, 0, 1)}])
+                                   {"schedule": (2048, 0, 1)}, {"schedule": (2048, 0, 2)}, {"schedule": (1024, 0, 4)},
+                                   {"schedule": (4096, 1, 6)}, {"schedule": (256, 0, 7)}])
 def test_gpu_schedules_and_streams_agree(knobs, gpu, oracle_bin):
     """Results never depend on how a level is scheduled: fan-in classes in
     turn or concurrently, link and copy per class or per level, the next
     level's plan beside the copies or after them, lanes per copied segment,
-    profiled runs, segments per SM, warp-per-segment classes."""
+    profiled runs, segments per SM, warp-per-segment classes, the gate
+    kernel's block size (flag 2) and load width (flag 4)."""
     nl, st = random_case(960, max_gates=120, max_in=8, horizon=20000, max_events=2000)
     ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
     env = {k: v for k, v in knobs.items() if k.startswith("GLS_")}
