@@ -536,18 +536,18 @@ def batched_arm(args):
     launches = sim.stats()["launches"]
     pool_b = sim.stats()["pool_bytes"]
     sim.close()
-    # The fixed cost of the launch sequence, which a persistent kernel could
-    # at most remove: the same windows cut to one cycle each, so every kernel
-    # of every level still launches (plan over all gates included) with next
-    # to no events.  Cost per launch, times this run's launches, against its
-    # device time.
+    # What a persistent kernel could at most remove: the launches themselves.
+    # One window of one cycle on the same netlist runs every kernel of every
+    # level with next to no work (the plan still reads one window's gates):
+    # its device time per launch bounds the cost of a launch from above;
+    # times this step's launches, against this step's device time.
     fixed = Simulator(device=local, alloc_mode=alloc)
     if args.alloc == "learned":
         fixed.set_presize_model(*presize.load(args.model or presize.DEFAULT_MODEL))
     fixed.load(nl)
     fixed.set_schedule(tune["best"]["seg_per_sm"], tune["best"]["warp_mask"], tune["best"]["flags"])
     one = synth.scaled(cfg, cycles=1)
-    tiny = [(synth.make_stimulus(one, nl.ppi_nets, seed=args.seed + 100 + k), one.t_end) for k in mine]
+    tiny = [(synth.make_stimulus(one, nl.ppi_nets, seed=args.seed + 100), one.t_end)]
     fixed_ms = fixed_launches = 0
     for rep in range(3):   # the first pass warms up
         fixed.clear_windows()
@@ -560,8 +560,9 @@ def batched_arm(args):
     launch_cost = {"per_launch_us": per_launch_us, "launches_per_step": int(launches),
                    "est_ms_per_step": per_launch_us * launches / 1000.0,
                    "share_of_device_time": per_launch_us * launches / 1000.0 / (dev_ms / args.steps),
-                   "what": "device time per launch of the same windows cut to one cycle (every kernel of every "
-                           "level launched, next to no events), times this step's launches"}
+                   "what": "device time per launch of one window of one cycle on the same netlist (every kernel "
+                           "of every level launched, next to no work): an upper bound of a launch's cost, times "
+                           "this step's launches"}
     # sequential plain runs of the same windows (exact allocation, one gls_run each)
     plain = Simulator(device=local, alloc_mode=ALLOC_EXACT)
     plain.load(nl)

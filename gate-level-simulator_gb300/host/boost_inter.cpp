@@ -672,8 +672,12 @@ void design_to_ref_inter(const Design &d, const Library &lib, ref::Inter &out, b
         r.name = in.name;
         const size_t ni = cell.inputs.size();
         std::vector<uint32_t> conn = in.conn;
-        if (conn.empty())
-            for (uint32_t k = 0; k < in.pins.size(); ++k) conn.push_back(k);
+        if (conn.empty())   // the native format keeps no port list: a port on its private open net was left open
+            for (uint32_t k = 0; k < in.pins.size(); ++k) {
+                const std::string &nm = net(in.pins[k]);
+                const bool open = k < ni ? nm == "gls_open_input" : nm == in.name + "[" + cell.outputs[k - ni] + "]";
+                if (!open) conn.push_back(k);
+            }
         for (uint32_t port : conn) {
             const std::string &nm = net(in.pins[port]);
             if (port < ni) {

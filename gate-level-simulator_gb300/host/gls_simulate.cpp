@@ -19,6 +19,7 @@
 // given; both read the same changes.  A binary stimulus file written by
 // gls_vcd2stim (it starts "GLSSTIM1") may stand in for the VCD: its change
 // lists are loaded as they are.
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -85,6 +86,9 @@ int main(int argc, char **argv)
         printf("dumpoff_time must be greater than dumpon_time\n");
         return 255;
     }
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    auto ms_since = [](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
     std::string err;
     Design d;
     ref::Inter archived;   // the reference's content of the design (for --saif-order=ref)
@@ -102,6 +106,8 @@ int main(int argc, char **argv)
             return 255;
         }
     }
+    const double ms_design = ms_since(t_start);
+    const auto t_vcd = clk::now();
     VcdData vcd;
     const std::string vtext = read_file(argv[2], &err);
     if (vtext.empty() ||
@@ -220,6 +226,8 @@ int main(int argc, char **argv)
         printf("ERROR: no usable CUDA device (gls_create %d)\n", rc);
         return 255;
     }
+    const double ms_stim = ms_since(t_vcd);
+    const auto t_run = clk::now();
     uint32_t win = 0;
     if ((rc = gls_load_netlist(ctx, &nl)) || (rc = gls_add_window(ctx, &st, t_begin, t_end, &win)) || (rc = gls_run(ctx))) {
         printf("ERROR: %s\n", gls_last_error(ctx));
@@ -231,6 +239,8 @@ int main(int argc, char **argv)
     gls_stats stats;
     gls_stats_get(ctx, &stats);
     gls_destroy(ctx);
+    const double ms_run = ms_since(t_run);
+    const auto t_saif = clk::now();
     // SAIF text, format of src/simulate.cu:457-481
     const unsigned long long dur = t_end - t_begin;
     outf << "(TIMESCALE " << vcd.time_res << " " << vcd.time_unit << ")\n";
@@ -317,5 +327,7 @@ int main(int argc, char **argv)
     printf("simulated %zu instances in %zu levels: %llu gate-events, %llu output events, %.3f ms on the GPU\n",
            d.insts.size(), d.level_start.size() - 1, (unsigned long long)stats.gate_events,
            (unsigned long long)stats.output_events, stats.kernel_ms);
+    printf("timing (ms): design %.1f, stimulus %.1f, simulate %.1f (GPU kernels %.1f), SAIF %.1f, total %.1f\n",
+           ms_design, ms_stim, ms_run, stats.kernel_ms, ms_since(t_saif), ms_since(t_start));
     return 0;
 }

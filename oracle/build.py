@@ -8,6 +8,11 @@
    oracle/ref_levels_driver.cpp.
 4. oracle/_ref/ref_vcd      -- the reference's VCD reader (src/VCDParser.cpp and
    src/VCDValue.cpp as they are) with oracle/ref_vcd_driver.cpp.
+5. oracle/_ref/ref_gpu_sim  -- the reference's GPU `simulate` tool (src/simulate.cu
+   with its reader sources, as they are) for sm_103a, with the text-archive
+   reader of oracle/boost_archive standing in for Boost: the reference GPU
+   tool timed on the same GPU (it is not a parity oracle: it deviates from
+   the serial core).
    Recipe: take src/simulate.cpp of the reference up to its `main` (which
    does not compile against the shipped VCDParser), rename its `calc` so
    oracle/ref_driver.cpp can choose the calc mode, and compile it with the
@@ -29,13 +34,14 @@ BUILD = ORACLE / "_build"
 REF = ORACLE / "_ref"
 REF_SRC = REF / "src"
 REFERENCE = Path(os.environ.get("GLS_REFERENCE", "/root/reference"))
-REF_HEADERS = ["VCDTypes.h", "Function.h", "Instance.h", "PreProcess.h", "VCDValue.h", "VCDParser.h"]
-REF_SOURCES = ["VCDParser.cpp", "VCDValue.cpp"]
+REF_HEADERS = ["VCDTypes.h", "Function.h", "Instance.h", "PreProcess.h", "VCDValue.h", "VCDParser.h", "simulate.cuh"]
+REF_SOURCES = ["VCDParser.cpp", "VCDValue.cpp", "simulate.cu", "PreProcess.cpp"]
 
 ORACLE_BIN = BUILD / "gls_oracle"
 REF_BIN = REF / "ref_sim"
 REF_LEVELS_BIN = REF / "ref_levels"
 REF_VCD_BIN = REF / "ref_vcd"
+REF_GPU_BIN = REF / "ref_gpu_sim"
 
 
 def _run(cmd):
@@ -102,6 +108,20 @@ def _build_ref_tool(exe: Path, srcs: list[Path], force: bool):
     if force or not exe.exists() or any(exe.stat().st_mtime < p.stat().st_mtime for p in srcs):
         _run(["g++", "-O2", "-std=c++17", "-DNDEBUG", "-pthread", "-w", f"-I{ORACLE / 'boost_stub'}", f"-I{REF_SRC}",
               "-o", str(exe), *map(str, srcs)])
+
+
+def build_reference_gpu(force: bool = False) -> Path | None:
+    """Build oracle/_ref/ref_gpu_sim (nvcc, sm_103a); None without the sources."""
+    if not (REF_SRC / "simulate.cu").exists() and not extract_reference():
+        return None
+    srcs = [REF_SRC / "simulate.cu", REF_SRC / "VCDParser.cpp", REF_SRC / "VCDValue.cpp", REF_SRC / "PreProcess.cpp"]
+    stub = ORACLE / "boost_archive"
+    deps = srcs + list((stub / "boost" / "archive").glob("*.hpp"))
+    if force or not REF_GPU_BIN.exists() or any(REF_GPU_BIN.stat().st_mtime < d.stat().st_mtime for d in deps):
+        nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+        _run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-w", "-DNDEBUG",
+              f"-I{stub}", f"-I{REF_SRC}", "-o", str(REF_GPU_BIN), *map(str, srcs)])
+    return REF_GPU_BIN
 
 
 def build_all(force: bool = False):
