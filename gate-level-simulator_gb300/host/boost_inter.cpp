@@ -43,7 +43,14 @@ const char kSignature[] = "serialization::archive";
 // Class types are told apart by name only, so the names must be unique per
 // C++ type; they never appear in the archive.
 template <class T> struct Key;
-#define GLS_KEY(T, S) template <> struct Key<T> { static std::string get() { return S; } };
+#define GLS_KEY(T, S)                                \
+    template <> struct Key<T> {                      \
+        static const std::string &get()              \
+        {                                            \
+            static const std::string k = S;          \
+            return k;                                \
+        }                                            \
+    };
 GLS_KEY(int, "int")
 GLS_KEY(uint32_t, "unsigned")
 GLS_KEY(int16_t, "short")
@@ -61,26 +68,56 @@ GLS_KEY(ref::PreProcess, "PreProcess")
 GLS_KEY(ref::Inter, "inter")
 #undef GLS_KEY
 template <class T> struct Key<std::vector<T>> {
-    static std::string get() { return "vector<" + Key<T>::get() + ">"; }
+    static const std::string &get()
+    {
+        static const std::string k = "vector<" + Key<T>::get() + ">";
+        return k;
+    }
 };
 template <class K, class V> struct Key<std::map<K, V>> {
-    static std::string get() { return "map<" + Key<K>::get() + "," + Key<V>::get() + ">"; }
+    static const std::string &get()
+    {
+        static const std::string k = "map<" + Key<K>::get() + "," + Key<V>::get() + ">";
+        return k;
+    }
 };
-const char kPinbitMap[] = "map<string,TimedValues*>";
-const char kPinbitPair[] = "pair<string,TimedValues*>";
-const char kTimedValues[] = "deque<TimedValue>";
+template <class K, class V> struct PairKey {
+    static const std::string &get()
+    {
+        static const std::string k = "pair<" + Key<K>::get() + "," + Key<V>::get() + ">";
+        return k;
+    }
+};
+// Every type key is one static string: the registry tells types apart by
+// the key's address.
+const std::string kPinbitMap = "map<string,TimedValues*>";
+const std::string kPinbitPair = "pair<string,TimedValues*>";
+const std::string kTimedValues = "deque<TimedValue>";
+const std::string kVectorVCDBit = "vector<VCDBit>";
 
 // ------------------------------------------------------------ archives
 struct Registry {
-    std::unordered_map<std::string, int> id;   // class number by type name
-    std::vector<char> tracked;                 // by class number
-    // first use of a type: give it the next number; true if new
-    bool first_use(const std::string &k)
+    std::unordered_map<const std::string *, int> id;   // class number by type key
+    std::vector<char> tracked;                         // by class number
+    // the class number of a type; *fresh is set on its first use, which
+    // gives it the next number
+    int use(const std::string &k, bool *fresh)
     {
-        if (id.count(k)) return false;
-        id.emplace(k, (int)tracked.size());
+        const auto it = id.find(&k);
+        if (it != id.end()) {
+            *fresh = false;
+            return it->second;
+        }
+        const int c = (int)tracked.size();
+        id.emplace(&k, c);
         tracked.push_back(0);
-        return true;
+        *fresh = true;
+        return c;
+    }
+    int find(const std::string &k) const
+    {
+        const auto it = id.find(&k);
+        return it == id.end() ? -1 : it->second;
     }
 };
 
@@ -132,13 +169,13 @@ struct Saver {
         out += s;
     }
     // class information of a type's first object
-    void class_info(const std::string &, int tracking)
+    void class_info(int, int tracking)
     {
         int t = tracking, v = 0;
         integer(t);
         integer(v);
     }
-    bool tracked(const std::string &) const { return false; }
+    bool tracked(int) const { return false; }
     void fail(const std::string &) { ok = false; }
 };
 
@@ -156,39 +193,43 @@ struct Loader {
         if (ok) err = m;
         ok = false;
     }
-    bool word(std::string &w)
+    static bool space(char c) { return c == ' ' || c == '\n' || c == '\r' || c == '\t'; }
+    // the next token, in place: [*b, *n)
+    bool word(const char *&b, const char *&n)
     {
-        while (p < e && (*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
-        const char *b = p;
-        while (p < e && !(*p == ' ' || *p == '\n' || *p == '\r' || *p == '\t')) ++p;
-        w.assign(b, p);
-        if (w.empty()) fail("archive ends early");
+        while (p < e && space(*p)) ++p;
+        b = p;
+        while (p < e && !space(*p)) ++p;
+        n = p;
+        if (b == n) fail("archive ends early");
         return ok;
     }
     template <class T> void integer(T &x)
     {
-        std::string w;
-        if (!word(w)) return;
-        char *end = nullptr;
-        errno = 0;
-        if (std::is_signed<T>::value) {
-            const long long v = strtoll(w.c_str(), &end, 10);
-            if (*end || errno) return fail("bad integer '" + w + "'");
-            x = (T)v;
-        } else {
-            if (w[0] == '-') return fail("negative count '" + w + "'");
-            const unsigned long long v = strtoull(w.c_str(), &end, 10);
-            if (*end || errno) return fail("bad integer '" + w + "'");
-            x = (T)v;
+        const char *b, *n;
+        if (!word(b, n)) return;
+        const char *q = b;
+        const bool neg = *q == '-';
+        if (neg) {
+            if (!std::is_signed<T>::value) return fail("negative count '" + std::string(b, n) + "'");
+            ++q;
         }
+        if (q == n || n - q > 20) return fail("bad integer '" + std::string(b, n) + "'");
+        unsigned long long v = 0;
+        for (; q < n; ++q) {
+            const unsigned d = (unsigned)(*q - '0');
+            if (d > 9 || v > (~0ull - d) / 10) return fail("bad integer '" + std::string(b, n) + "'");
+            v = v * 10 + d;
+        }
+        x = neg ? (T)(-(long long)v) : (T)v;
     }
     template <class T> void real(T &x)
     {
-        std::string w;
-        if (!word(w)) return;
+        const char *b, *n;
+        if (!word(b, n)) return;
         char *end = nullptr;
-        const double v = strtod(w.c_str(), &end);
-        if (*end) return fail("bad number '" + w + "'");
+        const double v = strtod(b, &end);   // stops at the delimiter after the token
+        if (end != n) return fail("bad number '" + std::string(b, n) + "'");
         x = (T)v;
     }
     void str(std::string &s)
@@ -206,14 +247,14 @@ struct Loader {
             s.clear();
         }
     }
-    void class_info(const std::string &k, int)
+    void class_info(int cid, int)
     {
         int tracking = 0, version = 0;
         integer(tracking);
         integer(version);
-        reg.tracked[reg.id[k]] = tracking != 0;
+        reg.tracked[cid] = tracking != 0;
     }
-    bool tracked(const std::string &k) { return reg.tracked[reg.id[k]] != 0; }
+    bool tracked(int cid) const { return reg.tracked[cid] != 0; }
     // a count that cannot exceed the bytes left (each element takes at least one)
     bool sane_count(uint64_t n)
     {
@@ -226,9 +267,11 @@ template <class A, class F>
 void object(A &a, const std::string &key, bool class_info, F &&body)
 {
     if (!a.ok) return;
-    if (a.reg.first_use(key) && class_info) a.class_info(key, 0);
+    bool fresh = false;
+    const int cid = a.reg.use(key, &fresh);
+    if (fresh && class_info) a.class_info(cid, 0);
     if (!a.ok) return;
-    if (A::kLoad && a.tracked(key)) {   // an archive that tracks this type numbers its objects
+    if (A::kLoad && a.tracked(cid)) {   // an archive that tracks this type numbers its objects
         uint32_t oid = 0;
         a.integer(oid);
     }
@@ -269,7 +312,7 @@ template <class A, class T> void io(A &a, std::vector<T> &v)
 
 template <class A, class K, class V> void io(A &a, std::map<K, V> &m)
 {
-    const std::string pair_key = "pair<" + Key<K>::get() + "," + Key<V>::get() + ">";
+    const std::string &pair_key = PairKey<K, V>::get();
     object(a, Key<std::map<K, V>>::get(), true, [&] {
         uint64_t n = m.size();
         count_and_version(a, n);
@@ -299,7 +342,7 @@ template <class A, class K, class V> void io(A &a, std::map<K, V> &m)
 
 template <class A> void io(A &a, ref::Pin &x)
 {
-    object(a, "Pin", true, [&] {
+    object(a, Key<ref::Pin>::get(), true, [&] {
         io(a, x.type);
         io(a, x.name);
         io(a, x.size);
@@ -309,14 +352,14 @@ template <class A> void io(A &a, ref::Pin &x)
 }
 template <class A> void io(A &a, ref::TimedValue &x)
 {
-    object(a, "TimedValue", true, [&] {
+    object(a, Key<ref::TimedValue>::get(), true, [&] {
         io(a, x.t);
         io(a, x.value);
     });
 }
 template <class A> void io(A &a, ref::Delay &x)
 {
-    object(a, "Delay", true, [&] {
+    object(a, Key<ref::Delay>::get(), true, [&] {
         io(a, x.edge);
         io(a, x.in_bit);
         io(a, x.out_bit);
@@ -326,13 +369,13 @@ template <class A> void io(A &a, ref::Delay &x)
 }
 template <class A> void io(A &a, ref::Function &x)
 {
-    object(a, "Function", true, [&] {
+    object(a, Key<ref::Function>::get(), true, [&] {
         io(a, x.name);
         io(a, x.id);
         io(a, x.input_pins);
         // std::vector<VCDBit>: a collection of an enum is not one of the
         // arithmetic collections, so it carries class information
-        object(a, "vector<VCDBit>", true, [&] {
+        object(a, kVectorVCDBit, true, [&] {
             uint64_t n = x.input_data.size();
             count_and_version(a, n);
             if (!a.ok) return;
@@ -345,7 +388,7 @@ template <class A> void io(A &a, ref::Function &x)
 }
 template <class A> void io(A &a, ref::ModuleType &x)
 {
-    object(a, "ModuleType", true, [&] {
+    object(a, Key<ref::ModuleType>::get(), true, [&] {
         io(a, x.name);
         io(a, x.ports);
         io(a, x.in_out_ports);
@@ -356,7 +399,7 @@ template <class A> void io(A &a, ref::ModuleType &x)
 }
 template <class A> void io(A &a, ref::Instance &x)
 {
-    object(a, "Instance", true, [&] {
+    object(a, Key<ref::Instance>::get(), true, [&] {
         io(a, x.type);
         io(a, x.name);
         io(a, x.in_port_net);
@@ -386,15 +429,16 @@ void load_pointed(Loader &l, std::vector<ref::TimedValue> &v, const std::string 
         v.clear();
         return;
     }
-    const auto it = l.reg.id.find(k);
-    if (it == l.reg.id.end()) {
+    const int known = l.reg.find(k);
+    if (known < 0) {
         if (cid != (int)l.reg.tracked.size()) return l.fail("unexpected class number " + std::to_string(cid));
-        l.reg.first_use(k);
-        l.class_info(k, 1);
-    } else if (it->second != cid) {
+        bool fresh = false;
+        l.reg.use(k, &fresh);
+        l.class_info(cid, 1);
+    } else if (known != cid) {
         return l.fail("pointer class number " + std::to_string(cid) + " is not the TimedValues class");
     }
-    if (!l.tracked(k)) return body();
+    if (!l.tracked(cid)) return body();
     uint32_t oid = 0;
     l.integer(oid);
     if (!l.ok) return;
@@ -412,7 +456,7 @@ void load_pointed(Loader &l, std::vector<ref::TimedValue> &v, const std::string 
 // TimedValue (a tracked class, since it is archived through pointers)
 template <class A> void io_pointed(A &a, std::vector<ref::TimedValue> &v)
 {
-    const std::string k = kTimedValues;
+    const std::string &k = kTimedValues;
     auto body = [&] {
         uint64_t n = v.size();
         count_and_version(a, n);
@@ -424,12 +468,12 @@ template <class A> void io_pointed(A &a, std::vector<ref::TimedValue> &v)
         }
     };
     if constexpr (!A::kLoad) {
-        const bool fresh = a.reg.first_use(k);
-        int cid = a.reg.id[k];
+        bool fresh = false;
+        int cid = a.reg.use(k, &fresh);
         a.integer(cid);
         if (fresh) {
             a.reg.tracked[cid] = 1;
-            a.class_info(k, 1);
+            a.class_info(cid, 1);
         }
         uint32_t oid = a.next_object++;
         a.integer(oid);
@@ -470,7 +514,7 @@ template <class A> void io_pinbits(A &a, std::map<std::string, std::vector<ref::
 
 template <class A> void io(A &a, ref::PreProcess &x)
 {
-    object(a, "PreProcess", true, [&] {
+    object(a, Key<ref::PreProcess>::get(), true, [&] {
         io(a, x.module_types);
         io(a, x.ignored_modules);
         io(a, x.top_module_name);
@@ -487,7 +531,7 @@ template <class A> void io(A &a, ref::PreProcess &x)
 }
 template <class A> void io(A &a, ref::Inter &x)
 {
-    object(a, "inter", true, [&] {
+    object(a, Key<ref::Inter>::get(), true, [&] {
         io(a, x.p);
         io(a, x.levels);
         io(a, x.initial_net_map);

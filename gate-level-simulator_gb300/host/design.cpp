@@ -36,14 +36,23 @@ int Design::find_net(const std::string &name) const
 
 std::string read_file(const std::string &path, std::string *err)
 {
-    std::ifstream f(path, std::ios::binary);
+    std::ifstream f(path, std::ios::binary | std::ios::ate);
     if (!f) {
         if (err) *err = "cannot open " + path;
         return std::string();
     }
-    std::ostringstream ss;
-    ss << f.rdbuf();
-    return ss.str();
+    // one read into a buffer of the file's size (files reach gigabytes)
+    const std::streamoff n = f.tellg();
+    std::string s;
+    if (n > 0) {
+        s.resize((size_t)n);
+        f.seekg(0);
+        if (!f.read(&s[0], n)) {
+            if (err) *err = "cannot read " + path;
+            return std::string();
+        }
+    }
+    return s;
 }
 
 namespace {

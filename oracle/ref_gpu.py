@@ -16,7 +16,7 @@ the reference prints its own phase times ("total time of simulating",
 "total time(all)"), gls_simulate its phase times and kernel time.
 
 Command line (one GPU):
-    python -m oracle.ref_gpu --config c1 [--cells N --depth D --cycles C] [--timeout S]
+    python -m oracle.ref_gpu --config c1 [--cells N --depth D --cycles C] [--timeout S] [--gls-only]
 """
 from __future__ import annotations
 
@@ -73,21 +73,23 @@ def compare_saif(a: str, b: str) -> dict:
             "differing": sum(ra[k] != rb[k] for k in common)}
 
 
-def run(d: Path, t_begin: int, t_end: int, timeout: float) -> dict:
+def run(d: Path, t_begin: int, t_end: int, timeout: float, reference: bool = True) -> dict:
     from gls import hostbuild
     from oracle import build
-    exe = build.build_reference_gpu()
-    if exe is None:
-        return {"unavailable": "the reference sources were not extracted (oracle/_ref/src)"}
     tools = hostbuild.build()
     res = {}
-    t0 = time.perf_counter()
-    r = subprocess.run([str(exe), str(d / "inter.dat"), str(d / "d.vcd"), str(t_begin), str(t_end),
-                        str(d / "ref.saif")], capture_output=True, text=True, timeout=timeout, cwd=d)
-    res["ref_wall_s"] = time.perf_counter() - t0
-    res["ref_rc"] = r.returncode
-    res["ref_ms"] = parse_ref_times(r.stdout)
-    (d / "ref.log").write_text(r.stdout + r.stderr)
+    r = None
+    if reference:
+        exe = build.build_reference_gpu()
+        if exe is None:
+            return {"unavailable": "the reference sources were not extracted (oracle/_ref/src)"}
+        t0 = time.perf_counter()
+        r = subprocess.run([str(exe), str(d / "inter.dat"), str(d / "d.vcd"), str(t_begin), str(t_end),
+                            str(d / "ref.saif")], capture_output=True, text=True, timeout=timeout, cwd=d)
+        res["ref_wall_s"] = time.perf_counter() - t0
+        res["ref_rc"] = r.returncode
+        res["ref_ms"] = parse_ref_times(r.stdout)
+        (d / "ref.log").write_text(r.stdout + r.stderr)
     t0 = time.perf_counter()
     g = subprocess.run([str(tools["gls_simulate"]), str(d / "inter.dat"), str(d / "d.vcd"), str(t_begin), str(t_end),
                         str(d / "gls.saif")], capture_output=True, text=True, timeout=timeout)
@@ -96,7 +98,7 @@ def run(d: Path, t_begin: int, t_end: int, timeout: float) -> dict:
     res["gls_ms"] = parse_gls_times(g.stdout)
     m = re.search(r"(\d+) gate-events", g.stdout)
     res["gate_events"] = int(m.group(1)) if m else None
-    if r.returncode == 0 and g.returncode == 0:
+    if r is not None and r.returncode == 0 and g.returncode == 0:
         res["saif"] = compare_saif((d / "ref.saif").read_text(), (d / "gls.saif").read_text())
     return res
 
@@ -110,6 +112,7 @@ def main():
     ap.add_argument("--cycles", type=int)
     ap.add_argument("--timeout", type=float, default=900)
     ap.add_argument("--dir", default="/tmp/gls_ref_gpu")
+    ap.add_argument("--gls-only", action="store_true", help="time gls_simulate alone (the reference tool is not run)")
     args = ap.parse_args()
     from gls import hostbuild, synth
     cfg = synth.CONFIGS[args.config]
@@ -122,7 +125,7 @@ def main():
     st = synth.make_stimulus(cfg, nl.ppi_nets, seed=args.seed)
     write_inputs(d, nl, st, hostbuild.build())
     prep = time.time() - t0
-    res = run(d, 0, cfg.t_end, args.timeout)
+    res = run(d, 0, cfg.t_end, args.timeout, reference=not args.gls_only)
     res.update({"workload": args.config, "cells": int(nl.n_inst), "levels": int(nl.n_levels),
                 "stimulus_events": int(st.n_events), "t_end": int(cfg.t_end), "inputs_written_s": prep})
     if res.get("gate_events") and res.get("ref_ms", {}).get("simulating"):
