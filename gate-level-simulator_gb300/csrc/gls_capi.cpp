@@ -68,6 +68,7 @@ void ctx_level_args(const gls_ctx *ctx, LevelArgs *a)
     a->bal_weight = ctx->bal_weight;
     a->wave_e = nullptr;
     a->wide = 0;
+    a->plan_part = 0;
 }
 
 namespace {
@@ -140,6 +141,7 @@ extern "C" int gls_create(const gls_opts *opts, gls_ctx **out)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->copy_ev[c], cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->slots_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stim_side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stim_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stim_join, cudaEventDisableTiming);
@@ -281,6 +283,7 @@ extern "C" int gls_destroy(gls_ctx *ctx)
         if (ctx->copy_ev[c]) cudaEventDestroy(ctx->copy_ev[c]);
     }
     if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+    if (ctx->slots_ev) cudaEventDestroy(ctx->slots_ev);
     if (ctx->stim_side) cudaStreamDestroy(ctx->stim_side);
     if (ctx->stim_fork) cudaEventDestroy(ctx->stim_fork);
     if (ctx->stim_join) cudaEventDestroy(ctx->stim_join);
@@ -828,13 +831,19 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
     // has linked (the plan needs the new lists' lengths and places, and
     // writes the other set of per-gate-output tables), while the copies
     // still run; a class's next simulation waits for every class's copy.
-    // Not in learned mode: the presize reads SAIF counts that the copies add.
+    // Learned mode splits the plan: the presize reads SAIF counts that the
+    // copies add, so the segments and stacks are planned beside the copies,
+    // and only the presize and the slot placement run between the copies
+    // and the next level's simulations.  (The learned balance sizes segments
+    // from the predictions: it keeps the plan whole, after the copies.)
+    const bool learned = a.alloc_mode == kAllocLearned;
+    const bool split = learned && ctx->bal_weight <= 0.f;
     const bool overlap_ok = ctx->concurrent && ctx->pipeline && ctx->plan_overlap && !(prof && ctx->opts.profile) &&
-                            a.alloc_mode != kAllocLearned;
+                            (!learned || split);
     if (prof) prof_mark(ctx);
-    if (overlap_ok) {
+    if (overlap_ok && !learned) {
         // the stimulus nets' SAIF beside the levels (nothing else reads or
-        // writes their counts; learned mode's presize would read them)
+        // writes their counts; learned mode's presize reads them)
         CK(cudaEventRecord(ctx->stim_fork, ctx->stream), "stim fork");
         CK(cudaStreamWaitEvent(ctx->stim_side, ctx->stim_fork, 0), "stim fork wait");
         launch_stim_saif(dw[0], *h[0], nwin, max_stim, w64, ctx->stim_side);
@@ -863,8 +872,12 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
             launch_wave_events(dwL, nwin, a, ctx->stream);
             ++*launches;
         }
-        if (a.alloc_mode == kAllocLearned) {
-            // the level's presize predictions (tensor cores) before its slots are planned
+        int n_cls = 0;
+        for (int c = 0; c < kClasses; ++c)
+            n_cls += ctx->cls_start[(kClasses + 1) * L + c + 1] > ctx->cls_start[(kClasses + 1) * L + c];
+        const bool overlap = overlap_ok && n_cls > 0;
+        const bool split_level = learned && overlap;
+        auto presize = [&]() {   // the level's presize predictions (tensor cores), before its slots are placed
             PresizeArgs pa;
             ctx_presize_args(ctx, &pa);
             pa.wv = dwL;
@@ -873,13 +886,12 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
             pa.n = a.hi - a.lo;
             launch_presize(pa, true, ctx->stream);
             ++*launches;
-        }
+        };
+        if (learned && !split_level) presize();
+        a.plan_part = split_level ? 1u : 0u;
         launch_plan(dwL, hL, nwin, a, ctx->stream);
+        a.plan_part = 0;
         if (prof) prof_mark(ctx);
-        int n_cls = 0;
-        for (int c = 0; c < kClasses; ++c)
-            n_cls += ctx->cls_start[(kClasses + 1) * L + c + 1] > ctx->cls_start[(kClasses + 1) * L + c];
-        const bool overlap = overlap_ok && n_cls > 0;
         // Concurrent: the fan-in classes simulate on their own streams, so
         // one class's blocks fill another's tail (linking and copying every
         // class together after the join measured faster than per class).
@@ -896,6 +908,18 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
                 for (int c2 = 0; c2 < kClasses; ++c2)
                     if (copied[c2]) CK(cudaStreamWaitEvent(st, ctx->copy_ev[c2], 0), "copy wait");
             }
+        }
+        if (split_level) {
+            // the presize and the slots after the previous level's copies
+            // (the main stream has waited for the links only)
+            for (int c2 = 0; c2 < kClasses; ++c2)
+                if (copied[c2]) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[c2], 0), "copy wait");
+            presize();
+            a.plan_part = 2;
+            launch_plan(dwL, hL, nwin, a, ctx->stream);
+            a.plan_part = 0;
+            ++*launches;
+            CK(cudaEventRecord(ctx->slots_ev, ctx->stream), "slots placed");
         }
         bool first = true;
         bool linked[kClasses] = {false, false, false, false};
@@ -914,6 +938,9 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
                 st = ctx->class_priority ? ctx->side_prio[c] : ctx->side[c];
                 CK(cudaStreamWaitEvent(st, ctx->fork_ev, 0), "fork wait");
             }
+            // the gate kernels fill every SM until their last segment: the
+            // presize and the slots go first, else they would wait for them
+            if (split_level) CK(cudaStreamWaitEvent(st, ctx->slots_ev, 0), "slots wait");
             launch_sim(dwL, hL, nwin, a, c, d0, d1, ctx->sm_count, st);
             ++*launches;
             if (fork && ctx->pipeline) {   // the class's link and copy right behind it
@@ -954,7 +981,7 @@ static int enqueue_levels(gls_ctx *ctx, const WinDev *const dw[2], const WinDev 
     // the last level's copies and the stimulus SAIF join the main stream
     for (int c = 0; c < kClasses; ++c)
         if (copied[c]) CK(cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[c], 0), "final join");
-    if (overlap_ok) CK(cudaStreamWaitEvent(ctx->stream, ctx->stim_join, 0), "stim join wait");
+    if (overlap_ok && !learned) CK(cudaStreamWaitEvent(ctx->stream, ctx->stim_join, 0), "stim join wait");
     CK(cudaGetLastError(), "kernel launch");
     return GLS_OK;
 }

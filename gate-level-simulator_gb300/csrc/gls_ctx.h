@@ -224,6 +224,7 @@ struct gls_ctx {
     cudaStream_t side_prio[gls::kClasses] = {};   // the same with priority rising with fan-in
     cudaEvent_t fork_ev = nullptr, join_ev[gls::kClasses] = {};
     cudaEvent_t link_ev[gls::kClasses] = {}, copy_ev[gls::kClasses] = {};
+    cudaEvent_t slots_ev = nullptr;          // learned mode, split plan: the level's slots are placed
     cudaStream_t stim_side = nullptr;        // the stimulus SAIF beside the first levels
     cudaEvent_t stim_fork = nullptr, stim_join = nullptr;
     bool plan_overlap = true;        // the next level's plan runs beside this level's copies (GLS_PLAN_OVERLAP)

@@ -194,6 +194,8 @@ struct LevelArgs {
     uint32_t wide;              // 1: the window holds 64-bit event words (one window per launch)
     uint32_t sim_variant;       // thread-per-segment gate kernel variant: bit 0 256-thread blocks, bit 1 wider loads
     float bal_weight;           // learned mode: segment work = fan-in events + bal_weight * predicted output events
+    uint32_t plan_part;         // k_plan: 0 all of it; learned mode split in two: 1 segments and stacks
+                                // (slots left open), 2 slot placement from the predictions
 };
 
 // Windows simulated together: every level kernel takes a device array of

@@ -245,6 +245,45 @@ __device__ void block_excl_scan3(uint32_t &x, unsigned long long &y, unsigned lo
 constexpr int kPlanPer = 4;
 
 // one block per window
+// Part 2 of a split plan (learned mode): every gate output's slot, sized
+// from its prediction once the presize has run, placed by a block scan;
+// the pool pointer moves only when the slots fit.  Part 1 left the gate
+// output's fan-in events in the slot table as E << 2 | class.  The segment
+// tables are already in use by the gate kernels: a failure only raises the
+// window's flag, and its link and copy skip it.
+__device__ void plan_slots(const WinDev &w, const LevelArgs &a, uint32_t n, uint32_t *sm32,
+                           unsigned long long *sm64, unsigned long long *sm64b)
+{
+    __shared__ unsigned long long s_top;
+    __shared__ bool s_skip;
+    if (threadIdx.x == 0) {
+        s_skip = *(volatile uint32_t *)w.err != 0;
+        s_top = *w.top;
+    }
+    __syncthreads();
+    if (s_skip) return;
+    const unsigned long long base = s_top;
+    unsigned long long run_slot = 0;
+    for (uint32_t r = 0; r < n; r += blockDim.x) {
+        const uint32_t i = r + threadIdx.x;
+        unsigned long long slot = 0;
+        if (i < n) {
+            const unsigned long long E = w.slot[i] >> 2;
+            slot = min((E + 1 + 3) & ~3ull, ((unsigned long long)w.pred[i] + 3) & ~3ull);
+            w.res[i] = (uint32_t)slot;
+        }
+        uint32_t xs = 0, tS;
+        unsigned long long xo = slot, xc = 0, tSlot, tScr;
+        block_excl_scan3(xs, xo, xc, tS, tSlot, tScr, sm32, sm64, sm64b);
+        if (i < n) w.slot[i] = base + run_slot + xo;
+        run_slot += tSlot;
+    }
+    if (threadIdx.x == 0) {
+        if (base + run_slot > w.cap) atomicOr(w.err, kErrPool);
+        else *w.top = base + run_slot;
+    }
+}
+
 template <bool kBatch>
 __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArgs a)
 {
@@ -256,6 +295,10 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
     __shared__ unsigned long long s_base;
     const WinDev &w = ws.get(blockIdx.x);
     const uint32_t n = a.hi - a.lo;
+    if (a.plan_part == 2) {
+        plan_slots(w, a, n, sm32, sm64, sm64b);
+        return;
+    }
     if (*w.err) {   // a failed window: an empty segment table keeps the later kernels off it
         for (uint32_t i = threadIdx.x; i <= n; i += blockDim.x) w.seg_base[i] = 0;
         if (threadIdx.x == 0) *w.n_segs = 0;
@@ -268,7 +311,7 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
     // segments are cut to equal work, so gates that change their output
     // often get more, shorter segments and the lanes of a warp finish
     // together.
-    const bool bal = a.alloc_mode == kAllocLearned && a.bal_weight > 0.f;
+    const bool bal = a.alloc_mode == kAllocLearned && a.bal_weight > 0.f && a.plan_part == 0;
     // Pass 1: every gate output's fan-in events E and fan-in class, parked
     // in its slot entry as E << 2 | class until pass 2 overwrites it; the
     // level's fan-in events per
@@ -349,7 +392,9 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         return;
     }
     // Pass 2: segments, slot and scratch sizes, placed by a block scan in
-    // gate-output order
+    // gate-output order (part 1: no slots; the parked E << 2 | class stays
+    // in the slot table for part 2)
+    const bool slots = a.plan_part != 1;
     const unsigned long long base = s_base;
     uint32_t run_seg = 0;
     unsigned long long run_slot = 0, run_scr = 0;
@@ -369,9 +414,9 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
                 S = (uint32_t)min((float)E, max(1.f, min(sf, (float)((E + seg - 1) / seg) * 4.f)));
             }
             slot = (E + 1 + 3) & ~3ull;     // final list: at most one event per step plus (0, X)
-            if (a.alloc_mode == kAllocExact) slot = 0;
+            if (a.alloc_mode == kAllocExact || !slots) slot = 0;
             else if (a.alloc_mode == kAllocLearned) slot = min(slot, ((unsigned long long)w.pred[i] + 3) & ~3ull);
-            if (a.alloc_mode != kAllocBound) w.res[i] = (uint32_t)slot;
+            if (a.alloc_mode != kAllocBound && slots) w.res[i] = (uint32_t)slot;
             scr = (E + S + 3) & ~3ull;      // segment stacks: events of the segment (+1 for the first)
         }
         uint32_t xs = S, tS;
@@ -379,7 +424,7 @@ __global__ void __launch_bounds__(1024) k_plan(const WinSet<kBatch> ws, LevelArg
         block_excl_scan3(xs, xo, xc, tS, tSlot, tScr, sm32, sm64, sm64b);
         if (i < n) {
             w.seg_base[i] = run_seg + xs;
-            w.slot[i] = base + run_slot + xo;
+            if (slots) w.slot[i] = base + run_slot + xo;
             w.scr[i] = run_scr + xc;
         }
         run_seg += tS;

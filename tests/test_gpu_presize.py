@@ -159,3 +159,24 @@ def test_trained_presize_gains_over_bound_allocation(gpu):
     n_drv = len(c)
     assert learned["presize_overflows"] <= 0.02 * n_drv
     assert q["overflow_rate"] <= 0.02 and q["mae_log"] < 0.2, q
+
+
+@pytest.mark.parametrize("knobs", [{}, {"GLS_PLAN_OVERLAP": "0"}, {"GLS_SIM_CONCURRENT": "0"},
+                                   {"GLS_BALANCE_WEIGHT": "1"}, {"GLS_SIM_PIPELINE": "0"}])
+def test_learned_mode_stream_orders_agree(knobs, gpu, oracle_bin):
+    """Learned allocation in every stream order: the split plan (segments
+    beside the previous level's copies, then the presize and the slots; the
+    default), the whole plan after the copies (no plan overlap, no
+    concurrent classes, no per-class pipeline) and the learned balance,
+    which keeps the plan whole.  Some slots too short, some not."""
+    from gpu_util import simulator
+    nl, st = random_case(960, max_gates=120, max_in=8, horizon=20000, max_events=2000)
+    ow, osaif, _ = run_oracle(nl, st, 100, 15000, threads=4)
+    with simulator(None, knobs, alloc_mode=ALLOC_LEARNED) as s:
+        s.set_presize_model(constant_model(3.0), margin=0.0, slack=1)
+        s.load(nl)
+        w = s.add_window(st, 100, 15000)
+        s.run()
+        gw = {n: s.waveform(n, w) for n in ow}
+        assert_same(gw, s.saif(w), ow, osaif, str(knobs))
+        assert s.stats()["presize_overflows"] > 0
