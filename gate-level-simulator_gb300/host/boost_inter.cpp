@@ -963,6 +963,11 @@ bool ref_inter_to_design(const ref::Inter &in, Design &d, std::string *err)
     d = Design();
     const ref::PreProcess &p = in.p;
     d.top = p.top_module_name;
+    {   // about one net per instance output plus the declared bits: no rehash while the names go in
+        const size_t nets = p.out_net_from_id.size() + p.pin_bits.size() + p.net_instance_map.size() + 16;
+        d.net_id.reserve(nets);
+        d.net_names.reserve(nets);
+    }
     for (const std::string &b : p.pin_bits) {
         const uint32_t id = d.net(b);
         if (b.find('[') != std::string::npos) d.bus_bits.push_back(id);
