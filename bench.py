@@ -633,7 +633,7 @@ def main():
                     help="c1-c3: fixed schedule 'segments_per_sm,warp_mask,flags' instead of autotuning")
     ap.add_argument("--parity-gates", type=int, default=2000,
                     help="gates of the sample checked against the reference core (and timed as the CPU baseline)")
-    ap.add_argument("--ref-budget", type=float, default=4.0,
+    ap.add_argument("--ref-budget", type=float, default=6.0,
                     help="reference arm: seconds of CPU work per step (the sample is sized to it)")
     args = ap.parse_args()
     if args.warmup < 3:

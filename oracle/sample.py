@@ -74,7 +74,14 @@ def run_sample(nl, waves_of, gates, t_begin, t_end, threads):
     from .runner import run_oracle, run_reference
     have_ref = build.build_reference() is not None
     run = run_reference if have_ref else run_oracle
-    snl, sst, gev, outs = sample_case(nl, waves_of, np.sort(np.asarray(gates)))
+    # the heaviest gates first (fan-in events of their distinct input nets):
+    # the threads take gates in this order, so the last ones to start are
+    # short and the threads finish together
+    gates = np.sort(np.asarray(gates))
+    work = np.array([sum(len(waves_of(int(n))[0]) for n in np.unique(nl.inputs_of(int(i)))) for i in gates],
+                    np.int64)
+    gates = gates[np.argsort(-work, kind="stable")]
+    snl, sst, gev, outs = sample_case(nl, waves_of, gates)
     waves, saif, sec = run(snl, sst, t_begin, t_end, threads=threads)
     return dict(rate=gev / sec, sec=sec, gates=len(gates), gev=gev, kind="reference" if have_ref else "port",
                 snl=snl, sst=sst, outs=outs, waves=waves, saif=saif, run=run)
