@@ -215,3 +215,35 @@ def test_gpu_pool_regrowth(gpu, oracle_bin):
     gw, gs, _, stats = gpu_run(nl, st, 0, 4000, pool_events=64)
     assert stats["overflow_retries"] >= 1
     assert_same(gw, gs, ow, osaif, "regrowth")
+
+
+@pytest.mark.parametrize("seg", [0, 8, 13])
+@pytest.mark.parametrize("calc", [CALC_FIXED, CALC_LITERAL])
+def test_gpu_controlled_inputs(seg, calc, gpu, oracle_bin):
+    """Gates whose output a slow input controls (NAND/NOR/AND/OR at their
+    controlling value, AOI/OAI, a mux select) fed a fast input whose events
+    the kernels read past while the output cannot change: long runs, events
+    at the very time the slow input changes, X and Z on both, segments that
+    cut through the runs."""
+    cells = [("GEN_NAND2_D1", 2), ("GEN_NOR3_D1", 3), ("GEN_AND2_D1", 2), ("GEN_OR2_D1", 2), ("GEN_AOI21_D1", 3),
+             ("GEN_OAI21_D1", 3), ("GEN_MUX2_D1", 3), ("GEN_XOR2_D1", 2)]
+    from gls.cells import LIBRARY
+    insts = []
+    n_in = 3
+    for k, (name, n) in enumerate(cells):
+        c = LIBRARY[name]
+        ins = [0, 1, 2][:n] if k % 2 == 0 else [1, 0, 2][:n]
+        arcs = [(e, i, o, float(5 + 3 * k), float(7 + 2 * k)) for e, i, o in c.arcs]
+        insts.append((name, ins, [n_in + k], arcs))
+    nl = assemble(insts, n_nets=n_in + len(cells))
+    rng = np.random.default_rng(11)
+    slow = [(t, int(v)) for t, v in zip(range(0, 20000, 1000), rng.choice([0, 3, 0, 3, 1], 20))]
+    fast_t = sorted(set(rng.integers(0, 20000, 1500).tolist()) | {1000, 3000, 7000, 12000})
+    fast = [(t, int(v)) for t, v in zip(fast_t, rng.choice([0, 3, 0, 3, 1, 2], len(fast_t)))]
+    mid_t = sorted(set(rng.integers(0, 20000, 300).tolist()) | {3000, 12000})
+    mid = [(t, int(v)) for t, v in zip(mid_t, rng.choice([0, 3, 2], len(mid_t)))]
+    st = stimulus({0: slow, 1: fast, 2: mid})
+    cn = "literal" if calc == CALC_LITERAL else "fixed"
+    ow, osaif, _ = run_oracle(nl, st, 0, 21000, calc=cn)
+    gw, gs, _, _ = gpu_run(nl, st, 0, 21000, calc=calc, seg=seg, warp_mask=0)
+    assert_same(gw, gs, ow, osaif, f"controlled inputs seg {seg} calc {cn}")
