@@ -655,14 +655,20 @@ extern "C" int gls_add_window(gls_ctx *ctx, const gls_stimulus *st, uint64_t t_b
             const uint8_t *vv = st->value + a;
             Wd *o = hw + at[k];
             uint32_t ev = 0, et = 0, ew = 0, eo = 0;
-            for (uint64_t e = 0; e < cnt; ++e) {
+            if (cnt) {   // one pass over the times: the order check reads the word before from cache
+                ev |= vv[0] > 3 ? 1u : 0u;
+                ew |= tt[0] > kMaxTime ? 1u : 0u;
+                et |= tt[0] > kMaxTimeWide ? 1u : 0u;
+                o[0] = ((Wd)tt[0] << 2) | (Wd)(vv[0] & 3u);
+            }
+            for (uint64_t e = 1; e < cnt; ++e) {
                 const uint32_t t = tt[e], v = vv[e];
                 ev |= v > 3 ? 1u : 0u;
                 ew |= t > kMaxTime ? 1u : 0u;
                 et |= t > kMaxTimeWide ? 1u : 0u;
+                eo |= t <= tt[e - 1] ? 1u : 0u;
                 o[e] = ((Wd)t << 2) | (Wd)(v & 3u);
             }
-            for (uint64_t e = 1; e < cnt; ++e) eo |= tt[e] <= tt[e - 1] ? 1u : 0u;
             for (uint64_t e = cnt; e < round4(cnt); ++e) o[e] = EvW<Wd>::kInfW;
             if (ew) long_times = true;
             if (ev | et | eo) {
@@ -1441,6 +1447,23 @@ extern "C" int gls_autotune(gls_ctx *ctx, const gls_batch_opts *opts, gls_tune_r
     return GLS_OK;
 }
 
+// A large host copy split over the context's worker threads (the SAIF table
+// of a 2M-net design is 48 MB: one thread copies it at a fraction of the
+// memory bandwidth).
+static void host_copy(gls_ctx *ctx, void *dst, const void *src, size_t bytes)
+{
+    if (bytes < (8u << 20) || !ctx->pool) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const unsigned parts = ctx->pool->threads();
+    const size_t step = ((bytes + parts - 1) / parts + 63) & ~(size_t)63;
+    ctx->pool->parallel_for(parts, [&](unsigned q) {
+        const size_t a = std::min(bytes, q * step), b = std::min(bytes, a + step);
+        if (b > a) std::memcpy(static_cast<char *>(dst) + a, static_cast<const char *>(src) + a, b - a);
+    });
+}
+
 static Window *get_done(gls_ctx *ctx, uint32_t window)
 {
     if (window >= ctx->windows.size()) return nullptr;
@@ -1461,10 +1484,21 @@ extern "C" int gls_saif_counts(gls_ctx *ctx, uint32_t window, uint64_t *t0, uint
     CK(cudaMemcpyAsync(ctx->pin_out.p, w->saif.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "read saif");
     CK(cudaStreamSynchronize(ctx->stream), "read saif");
     const uint64_t *buf = ctx->pin_out.as<uint64_t>();
-    for (uint32_t n = 0; n < ctx->n_nets; ++n) {
-        t0[n] = buf[3ull * n];
-        t1[n] = buf[3ull * n + 1];
-        tx[n] = buf[3ull * n + 2];
+    auto part = [&](uint32_t n0, uint32_t n1) {
+        for (uint32_t n = n0; n < n1; ++n) {
+            t0[n] = buf[3ull * n];
+            t1[n] = buf[3ull * n + 1];
+            tx[n] = buf[3ull * n + 2];
+        }
+    };
+    if (ctx->n_nets < (1u << 18) || !ctx->pool) {
+        part(0, ctx->n_nets);
+    } else {   // large designs: split over the worker threads, like host_copy
+        const unsigned parts = ctx->pool->threads();
+        const uint32_t step = (ctx->n_nets + parts - 1) / parts;
+        ctx->pool->parallel_for(parts, [&](unsigned q) {
+            part(std::min(ctx->n_nets, q * step), std::min(ctx->n_nets, (q + 1) * step));
+        });
     }
     return GLS_OK;
 }
@@ -1480,7 +1514,7 @@ extern "C" int gls_saif_table(gls_ctx *ctx, uint32_t window, uint64_t *t3)
     if (!ctx->pin_out.ensure(bytes)) return fail(ctx, GLS_ENOMEM, "pinned staging for SAIF counts");
     CK(cudaMemcpyAsync(ctx->pin_out.p, w->saif.p, bytes, cudaMemcpyDeviceToHost, ctx->stream), "read saif");
     CK(cudaStreamSynchronize(ctx->stream), "read saif");
-    std::memcpy(t3, ctx->pin_out.p, bytes);
+    host_copy(ctx, t3, ctx->pin_out.p, bytes);
     return GLS_OK;
 }
 
