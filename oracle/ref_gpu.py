@@ -65,6 +65,26 @@ def parse_gls_times(text: str) -> dict:
     return dict(zip(("design", "stimulus", "simulate", "gpu_kernels", "saif", "total"), map(float, m.groups())))
 
 
+def record_names(text: str) -> list:
+    """NET record names of a SAIF file, in file order."""
+    lines = text.splitlines()
+    return [lines[k - 1].strip()[1:] for k, x in enumerate(lines) if re.match(r"\s*\(T0 \d+\)", x)]
+
+
+def compare_order(ref_text: str, gls_text: str) -> dict:
+    """The reference GPU tool's SAIF file against gls_simulate's
+    --saif-order=ref file: the record names in sequence, and the whole text
+    with the counts blanked (their values differ where the reference GPU
+    tool deviates from the serial core)."""
+    a, b = record_names(ref_text), record_names(gls_text)
+    k = 0
+    while k < min(len(a), len(b)) and a[k] == b[k]:
+        k += 1
+    blank = lambda t: re.sub(r"\((T0|T1|TX) \d+\)", r"(\1 _)", t)
+    return {"records_ref": len(a), "records_gls": len(b), "same_sequence": a == b,
+            "first_difference": None if a == b else k, "same_text_without_counts": blank(ref_text) == blank(gls_text)}
+
+
 def compare_saif(a: str, b: str) -> dict:
     from gls.files import parse_saif
     ra, rb = parse_saif(a), parse_saif(b)
@@ -100,6 +120,12 @@ def run(d: Path, t_begin: int, t_end: int, timeout: float, reference: bool = Tru
     res["gate_events"] = int(m.group(1)) if m else None
     if r is not None and r.returncode == 0 and g.returncode == 0:
         res["saif"] = compare_saif((d / "ref.saif").read_text(), (d / "gls.saif").read_text())
+        # the same files in the reference GPU tool's record order
+        o = subprocess.run([str(tools["gls_simulate"]), str(d / "inter.dat"), str(d / "d.vcd"), str(t_begin),
+                            str(t_end), str(d / "gls_ref_order.saif"), "--saif-order=ref"], capture_output=True,
+                           text=True, timeout=timeout)
+        if o.returncode == 0:
+            res["saif_order"] = compare_order((d / "ref.saif").read_text(), (d / "gls_ref_order.saif").read_text())
     return res
 
 
