@@ -44,6 +44,73 @@ def write_inputs(d: Path, nl, st, tools) -> None:
         raise RuntimeError(f"gls_process failed:\n{r.stdout}")
 
 
+# A small design that exercises what the generator's netlists do not: bus
+# ports, assign aliases and constants, pins tied off, an output left open,
+# a declared output bit nothing drives, input bits nothing reads, and VCD
+# signals the design does not have.
+BUS_GV = """module t (a, b, sel, d, o);
+input [7:0] a;
+input b, sel;
+input [3:0] d;
+wire [1:0] w;
+wire x, y, z, k0, k1;
+output [3:0] o;
+assign k0 = 1'b1;
+assign k1 = 1'b0;
+assign y = x;
+GEN_AND2_D1 U0 ( .a1(a[0]), .a2(a[1]), .z(x) );
+GEN_NOR2_D1 U1 ( .a1(y), .a2(b), .zn(w[0]) );
+GEN_MUX2_D1 U2 ( .i0(w[0]), .i1(a[3]), .s(sel), .z(w[1]) );
+GEN_NAND2_D1 U3 ( .a1(k0), .a2(w[1]), .zn(o[0]) );
+GEN_XOR2_D1 U4 ( .a1(1'b0), .a2(a[2]), .z(z) );
+GEN_INV_D1 U5 ( .i(z) );
+GEN_OR2_D1 U6 ( .a1(d[1]), .a2(a[5]), .z(o[2]) );
+GEN_NAND3_D1 U7 ( .a1(a[6]), .a2(a[7]), .a3(k1), .zn(o[3]) );
+endmodule
+"""
+BUS_SDF = """(DELAYFILE (TIMESCALE 1ps)
+ (CELL (CELLTYPE "GEN_AND2_D1") (INSTANCE U0) (DELAY (ABSOLUTE (IOPATH a1 z (11:11:11) (13:13:13)) (IOPATH a2 z (17:17:17) (19:19:19)))))
+ (CELL (CELLTYPE "GEN_NOR2_D1") (INSTANCE U1) (DELAY (ABSOLUTE (IOPATH a1 zn (5:5:5) (7:7:7)) (IOPATH a2 zn (9:9:9) (12:12:12)))))
+ (CELL (CELLTYPE "GEN_MUX2_D1") (INSTANCE U2) (DELAY (ABSOLUTE (IOPATH i0 z (20:20:20) (21:21:21)) (IOPATH i1 z (22:22:22) (23:23:23))
+    (IOPATH (posedge s) z (30:30:30) (31:31:31)) (IOPATH (negedge s) z (32:32:32) (33:33:33)))))
+ (CELL (CELLTYPE "GEN_NAND2_D1") (INSTANCE U3) (DELAY (ABSOLUTE (IOPATH a1 zn (8:8:8) (9:9:9)) (IOPATH a2 zn (10:10:10) (14:14:14)))))
+ (CELL (CELLTYPE "GEN_XOR2_D1") (INSTANCE U4) (DELAY (ABSOLUTE (IOPATH (posedge a1) z (4:4:4) (5:5:5)) (IOPATH (negedge a1) z (6:6:6) (7:7:7))
+    (IOPATH (posedge a2) z (8:8:8) (9:9:9)) (IOPATH (negedge a2) z (10:10:10) (11:11:11)))))
+ (CELL (CELLTYPE "GEN_INV_D1") (INSTANCE U5) (DELAY (ABSOLUTE (IOPATH i zn (3:3:3) (4:4:4)))))
+ (CELL (CELLTYPE "GEN_OR2_D1") (INSTANCE U6) (DELAY (ABSOLUTE (IOPATH a1 z (6:6:6) (8:8:8)) (IOPATH a2 z (7:7:7) (9:9:9)))))
+ (CELL (CELLTYPE "GEN_NAND3_D1") (INSTANCE U7) (DELAY (ABSOLUTE (IOPATH a1 zn (6:6:6) (7:7:7)) (IOPATH a2 zn (8:8:8) (9:9:9))
+    (IOPATH a3 zn (10:10:10) (11:11:11)))))
+)
+"""
+
+
+def bus_vcd(seed: int, n_times: int = 1500) -> str:
+    """A VCD for BUS_GV in the subset the reference's reader handles (every
+    change on its own line, full-width bus values, more than (2 x cores)^2
+    timestamps), with two signals the design does not have."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sigs = [("!", "a", 8), ('"', "b", 0), ("#", "sel", 0), ("$", "d", 4), ("%", "e", 0), ("&", "f", 2)]
+    head = ["$timescale 1ps $end", "$scope module t $end"]
+    head += [f"$var wire {max(w, 1)} {c} {n}{f' [{w - 1}:0]' if w else ''} $end" for c, n, w in sigs]
+    head += ["$upscope $end", "$enddefinitions $end"]
+    alpha = "01xz"
+
+    def val(w):
+        pick = lambda: alpha[int(rng.choice(4, p=[0.46, 0.46, 0.05, 0.03]))]   # noqa: E731
+        return pick() if w == 0 else "".join(pick() for _ in range(w))
+
+    body = ["#0", "$dumpvars"] + [val(w) + c if w == 0 else f"b{val(w)} {c}" for c, _, w in sigs] + ["$end"]
+    t = 0
+    for _ in range(n_times):
+        t += int(rng.integers(5, 60))
+        body.append(f"#{t}")
+        for j in rng.permutation(len(sigs))[: int(rng.integers(1, len(sigs) + 1))]:
+            c, _, w = sigs[int(j)]
+            body.append(val(w) + c if w == 0 else f"b{val(w)} {c}")
+    return "\n".join(head + body) + "\n", t
+
+
 def parse_ref_times(text: str) -> dict:
     """The phase times the reference GPU tool prints (milliseconds)."""
     keys = {"simulating": r"total time of simulating: (\d+)ms", "gpu": r"total time of gpu: (\d+)ms",
@@ -139,8 +206,27 @@ def main():
     ap.add_argument("--timeout", type=float, default=900)
     ap.add_argument("--dir", default="/tmp/gls_ref_gpu")
     ap.add_argument("--gls-only", action="store_true", help="time gls_simulate alone (the reference tool is not run)")
+    ap.add_argument("--design", default="generated", choices=["generated", "buses"],
+                    help="buses: the small bus / alias / constant design of this file instead of the generator's")
     args = ap.parse_args()
-    from gls import hostbuild, synth
+    from gls import files, hostbuild, synth
+    if args.design == "buses":
+        d = Path(args.dir)
+        d.mkdir(parents=True, exist_ok=True)
+        files.write_vlib(d / "lib.vlib")
+        (d / "d.gv").write_text(BUS_GV)
+        (d / "d.sdf").write_text(BUS_SDF)
+        text, t_last = bus_vcd(args.seed)
+        (d / "d.vcd").write_text(text)
+        tools = hostbuild.build()
+        r = subprocess.run([str(tools["gls_process"]), str(d / "lib.vlib"), str(d / "d.gv"), str(d / "d.sdf"),
+                            str(d / "inter.dat")], capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"gls_process failed:\n{r.stdout}")
+        res = run(d, 50, t_last + 100, args.timeout, reference=not args.gls_only)
+        res["workload"] = "buses"
+        print(json.dumps(res))
+        return
     cfg = synth.CONFIGS[args.config]
     if args.cells or args.depth or args.cycles:
         cfg = synth.scaled(cfg, cells=args.cells, depth=args.depth, cycles=args.cycles)
