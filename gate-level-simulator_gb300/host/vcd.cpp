@@ -264,6 +264,15 @@ int parse_vcd_gpu(const std::string &s, VcdData &v, std::string *err, int device
         parse_body(tk, v, vars);
         return 0;
     }
+    {   // room for every signal's changes up front: no regrowth while they go in
+        std::vector<uint64_t> cnt(v.names.size(), 0);
+        for (uint64_t r = 0; r < ch.n; ++r)
+            if (ch.value[r] != 255) ++cnt[ch.signal[r]];
+        for (size_t k = 0; k < cnt.size(); ++k) {
+            v.times[k].reserve(v.times[k].size() + cnt[k]);
+            v.values[k].reserve(v.values[k].size() + cnt[k]);
+        }
+    }
     Sink sink(v);
     for (uint64_t r = 0; r < ch.n; ++r)
         if (ch.value[r] != 255) sink.put(ch.signal[r], ch.value[r], ch.bus[r] != 0, ch.time[r]);
