@@ -438,7 +438,7 @@ def scaled_traffic(args, stats):
     """DRAM bytes of the gate kernels per step, scaled from an ncu capture
     of a smaller case of the same generator by the fan-in events processed
     (the kernels' traffic grows with the events they read and write)."""
-    tp = REPO / "profiles" / "k_sim_traffic.json"
+    tp = REPO / "profiles" / "k_sim_traffic_c3-100k-depth6-profiling-case.json"
     if not tp.exists() or args.cells or args.depth or args.cycles:
         return None, None
     tr = json.loads(tp.read_text())
